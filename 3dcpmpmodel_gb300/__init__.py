@@ -1,0 +1,182 @@
+"""GB300 chemical-potential multiphase D3Q19 MRT lattice-Boltzmann step.
+
+Python host side over the C ABI in ``include/cpmp.h`` (``libcpmp.so``, built
+in-tree by ``build.py``).  The names follow the reference program
+(zhou-yiling/3DCPMPmodel, FluidCuda.cu): ``Solver`` bundles what the
+reference's globals, ``Initialize``/``SetMultiphase``/``CudaInitialize``,
+``SetFlowField``, the step loop body and ``CalcMacroCPU``/``ContactAngle``
+did.  There is no CPU fallback: constructing a ``Solver`` loads the CUDA
+library and fails loudly if it is missing or no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import (CPMP_F32, CPMP_F64, FIELD, MODEL, SCHEME, STORE, WALL, CpmpError,
+                   Diag, Droplet, Params, lib)
+
+__all__ = ["Solver", "Params", "Droplet", "Diag", "CpmpError", "lib", "default_params",
+           "coexistence", "MODEL", "SCHEME", "STORE", "WALL", "FIELD", "reference_ts"]
+
+Q = 19
+
+
+def reference_ts(tau: float):
+    """MRT rates of the reference's Initialize (FluidCuda.cu:154-157)."""
+    ts = [1.0] * Q
+    for q in (2, 4, 6, 8):
+        ts[q] = 1.1
+    for q in (9, 11, 13, 14, 15):
+        ts[q] = 1.0 / tau
+    return ts
+
+
+def default_params(**kw) -> Params:
+    """cpmp_params_default() with keyword overrides (field names of cpmp_params)."""
+    p = Params()
+    lib().cpmp_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "ts":
+            for q in range(Q):
+                p.ts[q] = float(v[q])
+            p.ts_from_tau = 0
+        elif k == "cocurve_dir":
+            p.cocurve_dir = None if v is None else v.encode()
+        else:
+            if not hasattr(p, k):
+                raise AttributeError(f"cpmp_params has no field {k!r}")
+            setattr(p, k, v)
+    return p
+
+
+def coexistence(model: int, tr: float, eos_a=0.0, eos_b=0.0, eos_omega=0.0, cocurve_dir=None):
+    """SetMultiphase stand-alone: dict of den_g, den_l, A, B, Tc, Rc."""
+    out = [C.c_double() for _ in range(6)]
+    _abi.check(lib().cpmp_coexistence(int(model), float(tr), float(eos_a), float(eos_b),
+                                      float(eos_omega),
+                                      None if cocurve_dir is None else cocurve_dir.encode(),
+                                      *[C.byref(o) for o in out]))
+    return dict(zip(("den_g", "den_l", "A", "B", "Tc", "Rc"), [o.value for o in out]))
+
+
+class Solver:
+    """One simulation box on one GPU (a cpmp_handle)."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self.params = params if params is not None else default_params(**kw)
+        if params is not None and kw:
+            raise TypeError("give either a Params or keyword overrides")
+        self._lib = lib()
+        self._h = C.c_void_p()
+        _abi.check(self._lib.cpmp_create(C.byref(self.params), C.byref(self._h)))
+        p = self.params
+        self.dx, self.dy, self.dz = p.dx, p.dy, p.dz
+        self.n = p.dx * p.dy * p.dz
+        g, l, A, B, T, Rc = (C.c_double() for _ in range(6))
+        _abi.check(self._lib.cpmp_get_eos(self._h, C.byref(g), C.byref(l), C.byref(A), C.byref(B),
+                                          C.byref(T), C.byref(Rc)))
+        self.den_g, self.den_l, self.A, self.B, self.T, self.Rc = (g.value, l.value, A.value,
+                                                                   B.value, T.value, Rc.value)
+
+    # life cycle -----------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.cpmp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # reference operations ----------------------------------------------------------
+    def set_flow_field(self, radius=None, width=None, centre=None):
+        """SetFlowField: centre None -> the reference's placement (DX/2, DY/2, R+2)."""
+        d = Droplet()
+        d.radius = float(radius if radius is not None else 60.0)
+        d.width = float(width if width is not None else 10.0)
+        if centre is None:
+            d.ref_centre = 1
+        else:
+            d.ref_centre = 0
+            d.cx, d.cy, d.cz = (float(c) for c in centre)
+        _abi.check(self._lib.cpmp_init_droplet(self._h, C.byref(d)))
+        return self
+
+    def set_base_pt(self, base_pt: float):
+        _abi.check(self._lib.cpmp_set_base_pt(self._h, C.c_double(base_pt)))
+
+    def set_wall_field(self, wall: np.ndarray):
+        w = np.ascontiguousarray(wall, dtype=np.float64).reshape(-1)
+        _abi.check(self._lib.cpmp_set_wall_field(self._h, w.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 C.c_size_t(w.size)))
+
+    def step(self, n: int = 1):
+        _abi.check(self._lib.cpmp_step(self._h, int(n)))
+        return self
+
+    def sync(self):
+        _abi.check(self._lib.cpmp_sync(self._h))
+
+    def get(self, field: str, dtype=np.float64) -> np.ndarray:
+        f = FIELD[field]
+        comps = {"rho": 1, "mu": 1, "u": 3, "mv": 3, "force": 3, "dist": Q, "type": 1}[field]
+        if field == "type":
+            out = np.empty(self.n, np.uint8)
+            _abi.check(self._lib.cpmp_get_field(self._h, f, 0, out.ctypes.data_as(C.c_void_p),
+                                                C.c_size_t(out.nbytes)))
+            return out
+        dt = np.dtype(dtype)
+        out = np.empty(comps * self.n, dt)
+        code = CPMP_F64 if dt == np.float64 else CPMP_F32
+        _abi.check(self._lib.cpmp_get_field(self._h, f, code, out.ctypes.data_as(C.c_void_p),
+                                            C.c_size_t(out.nbytes)))
+        return out
+
+    def set(self, field: str, values: np.ndarray):
+        a = np.ascontiguousarray(values)
+        if a.dtype not in (np.float64, np.float32):
+            a = a.astype(np.float64)
+        code = CPMP_F64 if a.dtype == np.float64 else CPMP_F32
+        _abi.check(self._lib.cpmp_set_field(self._h, FIELD[field], code,
+                                            a.ctypes.data_as(C.c_void_p), C.c_size_t(a.nbytes)))
+
+    def reduce(self, allow_nonfinite: bool = False) -> dict:
+        """CalcMacroCPU + ContactAngle(0, DY/2) + the Laplace probe, on the device."""
+        d = Diag()
+        rc = self._lib.cpmp_reduce(self._h, C.byref(d))
+        if rc != 0 and not (allow_nonfinite and rc == _abi.CPMP_ERR_NONFINITE):
+            _abi.check(rc)
+        return {k: getattr(d, k) for k, _ in Diag._fields_}
+
+    # timing ------------------------------------------------------------------------
+    @property
+    def stream(self) -> int:
+        return self._lib.cpmp_stream(self._h) or 0
+
+    def kernel_timing(self, on: bool):
+        _abi.check(self._lib.cpmp_set_kernel_timing(self._h, 1 if on else 0))
+
+    def kernel_times(self) -> dict:
+        cap = 16
+        names = (C.c_char_p * cap)()
+        launches = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        k = self._lib.cpmp_kernel_times(self._h, names, launches, ms, cap)
+        return {names[i].decode(): (launches[i], ms[i]) for i in range(min(k, cap))}
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._lib.cpmp_launch_count(self._h))

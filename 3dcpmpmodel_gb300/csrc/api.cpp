@@ -1,0 +1,741 @@
+// api.cpp -- the C ABI (include/cpmp.h): handle life cycle, parameter
+// derivation, device memory, step dispatch (with CUDA-graph replay), field
+// transfer and reductions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cpmp.h"
+#include "eos.h"
+#include "kernels.h"
+
+using namespace cpmp;
+
+namespace {
+
+thread_local std::string g_err;
+
+cpmp_status fail(cpmp_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(CPMP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+}  // namespace
+
+struct cpmp_handle {
+    cpmp_params p{};
+    std::string cocurve;
+    int eos = 0;
+    double A = 0, B = 0, Tc = 0, Rc = 0, T = 0, den_g = 0, den_l = 0;
+    double ts[CPMP_Q] = {0};
+    long long n = 0;
+    cudaStream_t st = nullptr;
+    bool plain = true;
+    bool f64 = false;  // PLAIN with FP64 storage/arithmetic
+    uint8_t *type = nullptr;
+    void *rho = nullptr, *mu = nullptr, *u = nullptr, *mv = nullptr, *F = nullptr;
+    void *fb[2] = {nullptr, nullptr};
+    int cur = 0;
+    void *h = nullptr;
+    float *f0[2] = {nullptr, nullptr};
+    void *wall = nullptr;
+    double *partials = nullptr, *dout = nullptr;
+    long long step = 0;
+    bool initialised = false;
+    std::unique_ptr<LaunchHook> hook;
+    bool timing = false;
+    long long launches = 0;
+    FusedTile tile{8, 32, 16};
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    int launches_per_step = 0;
+};
+
+namespace {
+
+size_t real_size(const cpmp_handle *h) { return h->f64 ? sizeof(double) : sizeof(float); }
+
+template <class R>
+KParams<R> make_kparams(const cpmp_handle *h)
+{
+    KParams<R> k{};
+    k.dx = h->p.dx;
+    k.dy = h->p.dy;
+    k.dz = h->p.dz;
+    k.n = h->n;
+    k.wall_mode = h->p.wall_mode;
+    k.eos = h->eos;
+    k.lap_order = h->p.lap_order;
+    k.complex_bc = h->p.complex_bc;
+    k.qp = (h->p.k1 != 0.0 || h->p.k2 != 0.0) ? 1 : 0;
+    k.kk = (R)(h->p.k * h->p.k);
+    k.A = (R)h->A;
+    k.B = (R)h->B;
+    k.T = (R)h->T;
+    k.ka = (R)h->p.ka;
+    k.k1 = (R)h->p.k1;
+    k.k2 = (R)h->p.k2;
+    for (int q = 0; q < CPMP_Q; ++q) k.ts[q] = (R)h->ts[q];
+    k.wall = (const R *)h->wall;
+    return k;
+}
+
+void free_all(cpmp_handle *h)
+{
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    void *ptrs[] = {h->type, h->rho, h->mu, h->u, h->mv, h->F, h->fb[0], h->fb[1], h->h, h->f0[0], h->f0[1],
+                    h->wall, h->partials, h->dout};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    h->type = nullptr;
+    h->rho = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
+    h->f0[0] = h->f0[1] = nullptr;
+    h->partials = h->dout = nullptr;
+    if (h->st) cudaStreamDestroy(h->st);
+    h->st = nullptr;
+}
+
+cpmp_status dalloc(void **ptr, size_t bytes, const char *what)
+{
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(CPMP_ERR_NOMEM, std::string("cudaMalloc(") + what + ", " + std::to_string(bytes) +
+                                        " bytes): " + cudaGetErrorString(e));
+    }
+    return CPMP_OK;
+}
+
+// Heuristic default tile for the fused kernel (the autotuner refines it).
+FusedTile default_tile(const cpmp_params &p)
+{
+    int ty = 8, tz = 32;
+    if (p.dy <= 2) { ty = 1; tz = 128; }
+    else if (p.dy < 8) { ty = 4; tz = 32; }
+    if (p.dz <= 32 && p.dy >= 8) { ty = 8; tz = 32; }
+    const long long tiles = (long long)((p.dz + tz - 1) / tz) * ((p.dy + ty - 1) / ty);
+    // aim for >= 4 CTAs per SM on a 152-SM part, but march at least 8 planes
+    long long xl = (long long)p.dx * tiles / (4 * 152);
+    xl = std::max<long long>(8, std::min<long long>(64, xl));
+    xl = std::min<long long>(xl, p.dx);
+    return FusedTile{ty, tz, (int)xl};
+}
+
+cpmp_status upload_wall(cpmp_handle *h, const std::vector<double> &w)
+{
+    const size_t cnt = w.size();
+    if (h->f64) {
+        CK(cudaMemcpyAsync(h->wall, w.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    } else {
+        std::vector<float> tmp(cnt);
+        for (size_t i = 0; i < cnt; ++i) tmp[i] = (float)w[i];
+        CK(cudaMemcpyAsync(h->wall, tmp.data(), cnt * sizeof(float), cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return CPMP_OK;
+}
+
+// one time step, launched directly (no graph)
+void launch_one_step(cpmp_handle *h, LaunchHook *hook)
+{
+    if (h->plain) {
+        if (h->f64) {
+            auto k = make_kparams<double>(h);
+            plain_launch_step<double, double>(k, h->type, (double *)h->rho, (double *)h->mu, (double *)h->u,
+                                              (double *)h->F, (double *)h->mv, (const double *)h->fb[h->cur],
+                                              (double *)h->fb[1 - h->cur], h->st, hook);
+        } else {
+            auto k = make_kparams<float>(h);
+            plain_launch_step<float, float>(k, h->type, (float *)h->rho, (float *)h->mu, (float *)h->u,
+                                            (float *)h->F, (float *)h->mv, (const float *)h->fb[h->cur],
+                                            (float *)h->fb[1 - h->cur], h->st, hook);
+        }
+        h->cur ^= 1;
+    } else {
+        auto k = make_kparams<float>(h);
+        const int P = (int)(h->step & 1);
+        fused_launch_wall(k, (float *)h->rho, h->st, hook);
+        fused_launch_collide(h->p.storage, k, P, h->tile, h->h, h->f0[P], h->f0[1 - P], (const float *)h->rho,
+                             h->st, hook);
+        fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho, h->st, hook);
+    }
+    h->step += 1;
+    h->launches += h->launches_per_step;
+}
+
+bool step_parity_even(const cpmp_handle *h) { return h->plain ? h->cur == 0 : (h->step & 1) == 0; }
+
+cpmp_status ensure_graph(cpmp_handle *h)
+{
+    if (h->gexec) return CPMP_OK;
+    // a two-step graph starting at even parity
+    cudaGraph_t g = nullptr;
+    const long long save_step = h->step, save_launch = h->launches;
+    const int save_cur = h->cur;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    launch_one_step(h, nullptr);
+    launch_one_step(h, nullptr);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    h->step = save_step;
+    h->launches = save_launch;
+    h->cur = save_cur;
+    if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        h->gexec = nullptr;
+        return fail(CPMP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    return CPMP_OK;
+}
+
+template <class T>
+void convert_copy(const T *src, void *dst, int dtype, size_t cnt)
+{
+    if (dtype == CPMP_F64) {
+        double *d = (double *)dst;
+        for (size_t i = 0; i < cnt; ++i) d[i] = (double)src[i];
+    } else {
+        float *d = (float *)dst;
+        for (size_t i = 0; i < cnt; ++i) d[i] = (float)src[i];
+    }
+}
+
+// Device buffer of `cnt` reals (the handle's real type) to host, converting.
+cpmp_status d2h_real(cpmp_handle *h, const void *dsrc, size_t cnt, int dtype, void *hdst)
+{
+    const bool native = (h->f64 && dtype == CPMP_F64) || (!h->f64 && dtype == CPMP_F32);
+    if (native) {
+        CK(cudaMemcpyAsync(hdst, dsrc, cnt * real_size(h), cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        return CPMP_OK;
+    }
+    std::vector<unsigned char> tmp(cnt * real_size(h));
+    CK(cudaMemcpyAsync(tmp.data(), dsrc, tmp.size(), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->f64)
+        convert_copy((const double *)tmp.data(), hdst, dtype, cnt);
+    else
+        convert_copy((const float *)tmp.data(), hdst, dtype, cnt);
+    return CPMP_OK;
+}
+
+cpmp_status h2d_real(cpmp_handle *h, void *ddst, size_t cnt, int dtype, const void *hsrc)
+{
+    const bool native = (h->f64 && dtype == CPMP_F64) || (!h->f64 && dtype == CPMP_F32);
+    if (native) {
+        CK(cudaMemcpyAsync(ddst, hsrc, cnt * real_size(h), cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        return CPMP_OK;
+    }
+    std::vector<unsigned char> tmp(cnt * real_size(h));
+    if (h->f64) {
+        double *d = (double *)tmp.data();
+        for (size_t i = 0; i < cnt; ++i) d[i] = ((const float *)hsrc)[i];
+    } else {
+        float *d = (float *)tmp.data();
+        for (size_t i = 0; i < cnt; ++i) d[i] = (float)((const double *)hsrc)[i];
+    }
+    CK(cudaMemcpyAsync(ddst, tmp.data(), tmp.size(), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return CPMP_OK;
+}
+
+// FUSED scheme: evaluate mu, F, u and mv of the current state into the
+// (lazily allocated) diagnostic buffers.
+cpmp_status fused_diag_fields(cpmp_handle *h)
+{
+    const size_t n = (size_t)h->n;
+    cpmp_status s;
+    if (!h->mu && (s = dalloc(&h->mu, n * sizeof(float), "mu")) != CPMP_OK) return s;
+    if (!h->F && (s = dalloc(&h->F, 3 * n * sizeof(float), "F")) != CPMP_OK) return s;
+    if (!h->u && (s = dalloc(&h->u, 3 * n * sizeof(float), "u")) != CPMP_OK) return s;
+    if (!h->mv && (s = dalloc(&h->mv, 3 * n * sizeof(float), "mv")) != CPMP_OK) return s;
+    CK(cudaMemsetAsync(h->mu, 0, n * sizeof(float), h->st));
+    CK(cudaMemsetAsync(h->F, 0, 3 * n * sizeof(float), h->st));
+    CK(cudaMemsetAsync(h->u, 0, 3 * n * sizeof(float), h->st));
+    CK(cudaMemsetAsync(h->mv, 0, 3 * n * sizeof(float), h->st));
+    auto k = make_kparams<float>(h);
+    const int P = (int)(h->step & 1);
+    plain_launch_mu_force<float>(k, h->type, (float *)h->rho, (float *)h->mu, (float *)h->F, h->st);
+    fused_launch_velocity(h->p.storage, k, P, h->h, h->f0[P], (const float *)h->rho, (float *)h->u, h->st);
+    diag_launch_mv(h->type, (const float *)h->rho, (const float *)h->u, (const float *)h->F, (float *)h->mv,
+                   h->n, h->st);
+    h->launches += (h->p.wall_mode == 1 ? (h->p.complex_bc ? 3 : 1) : 0) + 4;
+    CK(cudaGetLastError());
+    return CPMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cpmp_last_error(void) { return g_err.c_str(); }
+
+void cpmp_params_default(cpmp_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dx = p->dy = p->dz = 64;
+    p->model = CPMP_MP_CPPRW;
+    p->tr = 0.7;
+    p->k = 0.2;
+    p->ka = 0.001;
+    p->k1 = 0.0;
+    p->k2 = 0.0;
+    p->tau = 0.8;
+    p->ts_from_tau = 1;
+    p->base_pt = -0.08;
+    p->wall_mode = CPMP_WALL_Z;
+    p->lap_order = 5;
+    p->complex_bc = 1;
+    p->storage = CPMP_STORE_F32;
+    p->scheme = CPMP_SCHEME_PLAIN;
+    p->device = 0;
+}
+
+cpmp_status cpmp_coexistence(int model, double tr, double eos_a, double eos_b, double eos_omega,
+                             const char *cocurve_dir, double *den_g, double *den_l, double *A, double *B,
+                             double *Tc, double *Rc)
+{
+    double a, b, tc, rc;
+    if (!eos_constants(model, tr, eos_a, eos_b, eos_omega, &a, &b, &tc, &rc))
+        return fail(CPMP_ERR_PARAM, "unsupported model id " + std::to_string(model) +
+                                        " (chemical-potential models 201..206)");
+    if (!(tr > 0.0 && tr < 1.0)) return fail(CPMP_ERR_PARAM, "T/Tc must lie in (0, 1)");
+    double g = 0, l = 0;
+    if (cocurve_dir) {
+        const int r = read_cocurve(cocurve_dir, model, tr, &g, &l);
+        if (r != 0)
+            return fail(CPMP_ERR_COCURVE, std::string("CoCurve table ") + (r == -2 ? "not found" : "has no row") +
+                                              " for T/Tc=" + std::to_string(tr) + " in " + cocurve_dir);
+        g *= rc;
+        l *= rc;
+    } else {
+        if (maxwell(eos_of_model(model), a, b, tr * tc, &g, &l) != 0)
+            return fail(CPMP_ERR_PARAM, "no coexistence at this temperature");
+    }
+    if (den_g) *den_g = g;
+    if (den_l) *den_l = l;
+    if (A) *A = a;
+    if (B) *B = b;
+    if (Tc) *Tc = tc;
+    if (Rc) *Rc = rc;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
+{
+    if (!pin || !out) return fail(CPMP_ERR_PARAM, "null argument");
+    *out = nullptr;
+    const cpmp_params &p = *pin;
+    if (p.dx < 1 || p.dy < 1 || p.dz < 1) return fail(CPMP_ERR_PARAM, "grid dimensions must be positive");
+    if ((long long)p.dx * p.dy * p.dz > (1LL << 34)) return fail(CPMP_ERR_PARAM, "grid too large");
+    if (p.wall_mode != CPMP_WALL_NONE && p.wall_mode != CPMP_WALL_Z) return fail(CPMP_ERR_PARAM, "wall_mode");
+    if (p.wall_mode == CPMP_WALL_Z && p.dz < 8) return fail(CPMP_ERR_PARAM, "walled box needs dz >= 8");
+    if (p.lap_order != 5 && p.lap_order != 7) return fail(CPMP_ERR_PARAM, "lap_order must be 5 or 7");
+    if (p.scheme == CPMP_SCHEME_PLAIN && p.storage != CPMP_STORE_F32 && p.storage != CPMP_STORE_F64)
+        return fail(CPMP_ERR_UNSUPPORTED, "PLAIN scheme stores FP32 or FP64 populations");
+    if (p.scheme == CPMP_SCHEME_FUSED && p.storage == CPMP_STORE_F64)
+        return fail(CPMP_ERR_UNSUPPORTED, "FUSED scheme stores FP32, FP16 or BF16 populations");
+    if (p.scheme != CPMP_SCHEME_PLAIN && p.scheme != CPMP_SCHEME_FUSED) return fail(CPMP_ERR_PARAM, "scheme");
+    if (!(p.tau > 0.5)) return fail(CPMP_ERR_PARAM, "tau must exceed 0.5");
+
+    std::unique_ptr<cpmp_handle> h(new cpmp_handle());
+    h->p = p;
+    if (p.cocurve_dir) {
+        h->cocurve = p.cocurve_dir;
+        h->p.cocurve_dir = h->cocurve.c_str();
+    }
+    h->eos = eos_of_model(p.model);
+    if (h->eos < 0) return fail(CPMP_ERR_PARAM, "unsupported model id " + std::to_string(p.model));
+    double g = 0, l = 0;
+    cpmp_status s = cpmp_coexistence(p.model, p.tr, p.eos_a, p.eos_b, p.eos_omega,
+                                     (p.den_g > 0 && p.den_l > 0) ? nullptr : h->p.cocurve_dir, &g, &l, &h->A,
+                                     &h->B, &h->Tc, &h->Rc);
+    if (s != CPMP_OK) return s;
+    if (p.den_g > 0 && p.den_l > 0) {
+        g = p.den_g;
+        l = p.den_l;
+    }
+    h->den_g = g;
+    h->den_l = l;
+    h->T = p.tr * h->Tc;
+    if (p.ts_from_tau) {
+        for (int q = 0; q < CPMP_Q; ++q) h->ts[q] = 1.0;  // FluidCuda.cu:154-157
+        h->ts[2] = h->ts[4] = h->ts[6] = h->ts[8] = 1.1;
+        h->ts[9] = h->ts[11] = h->ts[13] = h->ts[14] = h->ts[15] = 1.0 / p.tau;
+    } else {
+        for (int q = 0; q < CPMP_Q; ++q) h->ts[q] = p.ts[q];
+    }
+    h->n = (long long)p.dx * p.dy * p.dz;
+    h->plain = p.scheme == CPMP_SCHEME_PLAIN;
+    h->f64 = h->plain && p.storage == CPMP_STORE_F64;
+    const int wall_launches = p.wall_mode == CPMP_WALL_Z ? (p.complex_bc ? 3 : 1) : 0;
+    h->launches_per_step = wall_launches + (h->plain ? 4 : 2);
+
+    CK(cudaSetDevice(p.device));
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    const size_t n = (size_t)h->n, rs = real_size(h.get());
+    const size_t np = (size_t)p.dx * p.dy;
+    struct Guard {
+        cpmp_handle *h;
+        bool armed = true;
+        ~Guard()
+        {
+            if (armed) free_all(h);
+        }
+    } guard{h.get()};
+    if ((s = dalloc((void **)&h->type, n, "type")) != CPMP_OK) return s;
+    if ((s = dalloc(&h->rho, n * rs, "rho")) != CPMP_OK) return s;
+    if ((s = dalloc(&h->wall, 2 * np * rs, "wall")) != CPMP_OK) return s;
+    if ((s = dalloc((void **)&h->partials, 3 * sizeof(double) * diag_partial_blocks(h->n), "partials")) != CPMP_OK)
+        return s;
+    if ((s = dalloc((void **)&h->dout, 32 * sizeof(double), "dout")) != CPMP_OK) return s;
+    if (h->plain) {
+        if ((s = dalloc(&h->mu, n * rs, "mu")) != CPMP_OK) return s;
+        if ((s = dalloc(&h->u, 3 * n * rs, "u")) != CPMP_OK) return s;
+        if ((s = dalloc(&h->mv, 3 * n * rs, "mv")) != CPMP_OK) return s;
+        if ((s = dalloc(&h->F, 3 * n * rs, "F")) != CPMP_OK) return s;
+        if ((s = dalloc(&h->fb[0], CPMP_Q * n * rs, "f")) != CPMP_OK) return s;
+        if ((s = dalloc(&h->fb[1], CPMP_Q * n * rs, "f")) != CPMP_OK) return s;
+    } else {
+        const size_t hs = p.storage == CPMP_STORE_F32 ? 4 : 2;
+        if ((s = dalloc(&h->h, (CPMP_Q - 1) * n * hs, "h")) != CPMP_OK) return s;
+        if ((s = dalloc((void **)&h->f0[0], n * sizeof(float), "f0")) != CPMP_OK) return s;
+        if ((s = dalloc((void **)&h->f0[1], n * sizeof(float), "f0")) != CPMP_OK) return s;
+        CK(fused_setup_attributes());
+        h->tile = default_tile(p);
+    }
+    std::vector<double> w(2 * np, p.base_pt);
+    if ((s = upload_wall(h.get(), w)) != CPMP_OK) return s;
+    guard.armed = false;
+    *out = h.release();
+    return CPMP_OK;
+}
+
+void cpmp_destroy(cpmp_handle *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->p.device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    h->hook.reset();
+    free_all(h);
+    delete h;
+}
+
+cpmp_status cpmp_init_droplet(cpmp_handle *h, const cpmp_droplet *d)
+{
+    if (!h || !d) return fail(CPMP_ERR_PARAM, "null argument");
+    if (!(d->width > 0)) return fail(CPMP_ERR_PARAM, "droplet width must be positive");
+    CK(cudaSetDevice(h->p.device));
+    DropletDev dd{d->cx, d->cy, d->cz, d->radius, d->width, h->den_g, h->den_l, d->ref_centre};
+    const size_t n = (size_t)h->n, rs = real_size(h);
+    if (h->plain) {
+        CK(cudaMemsetAsync(h->F, 0, 3 * n * rs, h->st));
+        CK(cudaMemsetAsync(h->mv, 0, 3 * n * rs, h->st));
+        CK(cudaMemsetAsync(h->fb[1], 0, CPMP_Q * n * rs, h->st));
+        if (h->f64)
+            plain_launch_init<double, double>(make_kparams<double>(h), dd, h->type, (double *)h->rho,
+                                              (double *)h->mu, (double *)h->u, (double *)h->fb[0], h->st);
+        else
+            plain_launch_init<float, float>(make_kparams<float>(h), dd, h->type, (float *)h->rho, (float *)h->mu,
+                                            (float *)h->u, (float *)h->fb[0], h->st);
+        h->cur = 0;
+    } else {
+        CK(cudaMemsetAsync(h->f0[1], 0, n * sizeof(float), h->st));
+        fused_launch_init(h->p.storage, make_kparams<float>(h), dd, h->type, (float *)h->rho, h->f0[0], h->h,
+                          h->st);
+    }
+    h->launches += h->plain ? 1 : 2;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+    h->step = 0;
+    h->initialised = true;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_set_base_pt(cpmp_handle *h, double base_pt)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    CK(cudaSetDevice(h->p.device));
+    h->p.base_pt = base_pt;
+    std::vector<double> w(2 * (size_t)h->p.dx * h->p.dy, base_pt);
+    return upload_wall(h, w);
+}
+
+cpmp_status cpmp_set_wall_field(cpmp_handle *h, const double *host, size_t count)
+{
+    if (!h || !host) return fail(CPMP_ERR_PARAM, "null argument");
+    if (count != 2 * (size_t)h->p.dx * h->p.dy)
+        return fail(CPMP_ERR_SIZE, "wall field needs 2*DX*DY values");
+    CK(cudaSetDevice(h->p.device));
+    std::vector<double> w(host, host + count);
+    return upload_wall(h, w);
+}
+
+cpmp_status cpmp_step(cpmp_handle *h, int nsteps)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    if (nsteps < 0) return fail(CPMP_ERR_PARAM, "nsteps must be >= 0");
+    if (!h->initialised) return fail(CPMP_ERR_PARAM, "cpmp_init_droplet or cpmp_set_field(DIST) first");
+    CK(cudaSetDevice(h->p.device));
+    LaunchHook *hook = h->timing ? h->hook.get() : nullptr;
+    int left = nsteps;
+    if (hook || nsteps < 2) {
+        for (; left > 0; --left) launch_one_step(h, hook);
+        CK(cudaGetLastError());
+        return CPMP_OK;
+    }
+    if (!step_parity_even(h)) {
+        launch_one_step(h, nullptr);
+        --left;
+    }
+    if (left >= 2) {
+        cpmp_status s = ensure_graph(h);
+        if (s != CPMP_OK) return s;
+        while (left >= 2) {
+            CK(cudaGraphLaunch(h->gexec, h->st));
+            h->step += 2;
+            h->launches += 2LL * h->launches_per_step;
+            left -= 2;  // two lattice swaps leave h->cur unchanged
+        }
+    }
+    if (left == 1) launch_one_step(h, nullptr);
+    CK(cudaGetLastError());
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_sync(cpmp_handle *h)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    CK(cudaSetDevice(h->p.device));
+    CK(cudaStreamSynchronize(h->st));
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_get_field(cpmp_handle *h, cpmp_field f, int dtype, void *dst, size_t bytes)
+{
+    if (!h || !dst) return fail(CPMP_ERR_PARAM, "null argument");
+    CK(cudaSetDevice(h->p.device));
+    const size_t n = (size_t)h->n;
+    if (f == CPMP_FIELD_TYPE) {
+        if (bytes != n) return fail(CPMP_ERR_SIZE, "TYPE needs N bytes");
+        CK(cudaMemcpyAsync(dst, h->type, n, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        return CPMP_OK;
+    }
+    if (dtype != CPMP_F64 && dtype != CPMP_F32) return fail(CPMP_ERR_PARAM, "dtype");
+    const size_t es = dtype == CPMP_F64 ? 8 : 4;
+    size_t comps;
+    switch (f) {
+    case CPMP_FIELD_RHO:
+    case CPMP_FIELD_MU: comps = 1; break;
+    case CPMP_FIELD_U:
+    case CPMP_FIELD_MV:
+    case CPMP_FIELD_FORCE: comps = 3; break;
+    case CPMP_FIELD_DIST: comps = CPMP_Q; break;
+    default: return fail(CPMP_ERR_PARAM, "unknown field");
+    }
+    if (bytes != comps * n * es) return fail(CPMP_ERR_SIZE, "buffer size does not match the field");
+    CK(cudaStreamSynchronize(h->st));
+    if (h->plain) {
+        const void *src = f == CPMP_FIELD_RHO ? h->rho : f == CPMP_FIELD_MU ? h->mu : f == CPMP_FIELD_U ? h->u
+                        : f == CPMP_FIELD_MV ? h->mv : f == CPMP_FIELD_FORCE ? h->F : h->fb[h->cur];
+        return d2h_real(h, src, comps * n, dtype, dst);
+    }
+    // FUSED
+    if (f == CPMP_FIELD_RHO) return d2h_real(h, h->rho, n, dtype, dst);
+    if (f == CPMP_FIELD_DIST) {
+        void *tmp = nullptr;
+        cpmp_status s = dalloc(&tmp, CPMP_Q * n * es, "decode");
+        if (s != CPMP_OK) return s;
+        cudaMemsetAsync(tmp, 0, CPMP_Q * n * es, h->st);
+        const int P = (int)(h->step & 1);
+        fused_launch_decode(h->p.storage, make_kparams<float>(h), P, h->h, h->f0[P], tmp, dtype == CPMP_F64, h->st);
+        h->launches += 1;
+        cudaError_t e = cudaMemcpyAsync(dst, tmp, CPMP_Q * n * es, cudaMemcpyDeviceToHost, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("decode copy: ") + cudaGetErrorString(e));
+        return CPMP_OK;
+    }
+    cpmp_status s = fused_diag_fields(h);
+    if (s != CPMP_OK) return s;
+    const void *src = f == CPMP_FIELD_MU ? h->mu : f == CPMP_FIELD_U ? h->u : f == CPMP_FIELD_MV ? h->mv : h->F;
+    return d2h_real(h, src, comps * n, dtype, dst);
+}
+
+cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *src, size_t bytes)
+{
+    if (!h || !src) return fail(CPMP_ERR_PARAM, "null argument");
+    if (dtype != CPMP_F64 && dtype != CPMP_F32) return fail(CPMP_ERR_PARAM, "dtype");
+    CK(cudaSetDevice(h->p.device));
+    const size_t n = (size_t)h->n, es = dtype == CPMP_F64 ? 8 : 4;
+    if (!h->initialised) {
+        // tags and wall values come from the initialiser; a flat state first
+        cpmp_droplet d{0, 0, 0, 1, 1, 1};
+        cpmp_status s = cpmp_init_droplet(h, &d);
+        if (s != CPMP_OK) return s;
+    }
+    CK(cudaStreamSynchronize(h->st));
+    if (f == CPMP_FIELD_RHO) {
+        if (bytes != n * es) return fail(CPMP_ERR_SIZE, "RHO needs N values");
+        return h2d_real(h, h->rho, n, dtype, src);
+    }
+    if (f == CPMP_FIELD_U) {
+        if (!h->plain) return fail(CPMP_ERR_UNSUPPORTED, "FUSED scheme derives U from DIST");
+        if (bytes != 3 * n * es) return fail(CPMP_ERR_SIZE, "U needs 3N values");
+        return h2d_real(h, h->u, 3 * n, dtype, src);
+    }
+    if (f != CPMP_FIELD_DIST) return fail(CPMP_ERR_UNSUPPORTED, "settable fields: RHO, U, DIST");
+    if (bytes != CPMP_Q * n * es) return fail(CPMP_ERR_SIZE, "DIST needs 19N values");
+    if (h->plain) {
+        cpmp_status s = h2d_real(h, h->fb[h->cur], CPMP_Q * n, dtype, src);
+        if (s != CPMP_OK) return s;
+        if (h->f64)
+            plain_launch_macro<double, double>(make_kparams<double>(h), h->type, (const double *)h->fb[h->cur],
+                                               (double *)h->rho, (double *)h->u, h->st);
+        else
+            plain_launch_macro<float, float>(make_kparams<float>(h), h->type, (const float *)h->fb[h->cur],
+                                             (float *)h->rho, (float *)h->u, h->st);
+        h->launches += 1;
+    } else {
+        void *tmp = nullptr;
+        cpmp_status s = dalloc(&tmp, CPMP_Q * n * es, "encode");
+        if (s != CPMP_OK) return s;
+        cudaError_t e = cudaMemcpyAsync(tmp, src, CPMP_Q * n * es, cudaMemcpyHostToDevice, h->st);
+        const int P = (int)(h->step & 1);
+        auto k = make_kparams<float>(h);
+        if (e == cudaSuccess) {
+            fused_launch_encode(h->p.storage, k, P, h->h, h->f0[P], tmp, dtype == CPMP_F64, h->st);
+            fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, h->st, nullptr);
+            h->launches += 3;
+            e = cudaStreamSynchronize(h->st);
+        }
+        cudaFree(tmp);
+        if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("encode: ") + cudaGetErrorString(e));
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
+{
+    if (!h || !out) return fail(CPMP_ERR_PARAM, "null argument");
+    CK(cudaSetDevice(h->p.device));
+    std::memset(out, 0, sizeof(*out));
+    if (!h->plain) {
+        cpmp_status s = fused_diag_fields(h);
+        if (s != CPMP_OK) return s;
+    }
+    const int tier = h->p.dy / 2;
+    if (h->f64) {
+        diag_launch_mass<double>(h->type, (const double *)h->rho, (const double *)h->mv, h->n, h->partials,
+                                 h->dout, h->st);
+        if (h->p.dx >= 8 && h->p.dz >= 8)
+            diag_launch_contact_angle<double>((const double *)h->rho, h->p.dx, h->p.dy, h->p.dz, tier, h->den_g,
+                                              h->den_l, h->dout + 4, h->st);
+        diag_launch_laplace<double>((const double *)h->rho, h->p.dx, h->p.dy, h->p.dz, h->eos, h->A, h->B, h->T,
+                                    h->p.k * h->p.k, h->dout + 12, h->st);
+    } else {
+        diag_launch_mass<float>(h->type, (const float *)h->rho, (const float *)h->mv, h->n, h->partials, h->dout,
+                                h->st);
+        if (h->p.dx >= 8 && h->p.dz >= 8)
+            diag_launch_contact_angle<float>((const float *)h->rho, h->p.dx, h->p.dy, h->p.dz, tier, h->den_g,
+                                             h->den_l, h->dout + 4, h->st);
+        diag_launch_laplace<float>((const float *)h->rho, h->p.dx, h->p.dy, h->p.dz, h->eos, h->A, h->B, h->T,
+                                   h->p.k * h->p.k, h->dout + 12, h->st);
+    }
+    h->launches += 4;
+    double r[16] = {0};
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(r, h->dout, 16 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    out->mass = r[0];
+    out->max_speed = std::sqrt(r[1]);
+    out->nonfinite = r[2] != 0.0;
+    if (h->p.dx >= 8 && h->p.dz >= 8) {
+        out->ca_left = r[4];
+        out->ca_right = r[5];
+        out->ca_cap = r[6];
+        out->x_left = r[7];
+        out->x_right = r[8];
+        out->cap_h = r[9];
+        out->cap_l = r[10];
+    }
+    out->lap_r = r[12];
+    out->lap_dp = r[13];
+    out->lap_sigma = r[14];
+    out->step = h->step;
+    if (out->nonfinite) return fail(CPMP_ERR_NONFINITE, "NaN or negative density on a fluid node");
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_get_eos(cpmp_handle *h, double *den_g, double *den_l, double *A, double *B, double *T, double *Rc)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    if (den_g) *den_g = h->den_g;
+    if (den_l) *den_l = h->den_l;
+    if (A) *A = h->A;
+    if (B) *B = h->B;
+    if (T) *T = h->T;
+    if (Rc) *Rc = h->Rc;
+    return CPMP_OK;
+}
+
+void *cpmp_stream(cpmp_handle *h) { return h ? (void *)h->st : nullptr; }
+
+cpmp_status cpmp_set_kernel_timing(cpmp_handle *h, int on)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    CK(cudaSetDevice(h->p.device));
+    if (on) {
+        if (!h->hook) h->hook.reset(new LaunchHook());
+        h->hook->reset();
+        h->timing = true;
+    } else {
+        if (h->hook) h->hook->fold();
+        h->timing = false;
+    }
+    return CPMP_OK;
+}
+
+int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, double *ms, int cap)
+{
+    if (!h || !h->hook) return 0;
+    cudaSetDevice(h->p.device);
+    h->hook->fold();
+    int k = 0;
+    for (int c = 0; c < K_CLASSES; ++c) {
+        if (h->hook->launches[c] == 0) continue;
+        if (k < cap) {
+            if (names) names[k] = kernel_class_name(c);
+            if (launches) launches[k] = h->hook->launches[c];
+            if (ms) ms[k] = h->hook->ms[c];
+        }
+        ++k;
+    }
+    return k;
+}
+
+long long cpmp_launch_count(cpmp_handle *h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,330 @@
+// k_diag.cu -- device diagnostics: FP64 mass / max-speed / non-finite
+// reduction (CalcMacroCPU, FluidCuda.cu:1626-1657), the contact angle of the
+// x-z slice (ContactAngle, FluidCuda.cu:557-734) and the Laplace-law probe
+// (SaveDataOriDen, FluidCuda.cu:1159-1199).  All reductions are warp-shuffle
+// then shared memory, in a fixed order, so results are run-to-run identical.
+#include <cfloat>
+#include <climits>
+
+#include "kernels.h"
+
+namespace cpmp {
+
+namespace {
+constexpr int kRedThreads = 256;
+constexpr int kMaxRedBlocks = 1024;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_or(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v |= __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_min_i(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max_i(int v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+}  // namespace
+
+int diag_partial_blocks(long long n)
+{
+    long long b = (n + kRedThreads - 1) / kRedThreads;
+    if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kRedThreads) k_mass_partial(const uint8_t *__restrict__ type,
+                                                             const R *__restrict__ rho,
+                                                             const R *__restrict__ mv, long long n,
+                                                             double *__restrict__ part)
+{
+    double s = 0.0, mx = 0.0;
+    int bad = 0;
+    for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
+         I += (long long)gridDim.x * blockDim.x) {
+        if (type[I] != FLUID) continue;
+        const double d = (double)rho[I];
+        if (!(d >= 0.0)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
+        s += d;
+        if (mv) {
+            const double a = mv[I], b = mv[I + n], c = mv[I + 2 * n];
+            mx = fmax(mx, a * a + b * b + c * c);
+        }
+    }
+    __shared__ double ss[kRedThreads / 32], sm[kRedThreads / 32];
+    __shared__ int sb[kRedThreads / 32];
+    s = warp_sum(s);
+    mx = warp_max(mx);
+    bad = warp_or(bad);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        ss[w] = s;
+        sm[w] = mx;
+        sb[w] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ts = 0.0, tm = 0.0;
+        int tb = 0;
+        for (int k = 0; k < kRedThreads / 32; ++k) {
+            ts += ss[k];
+            tm = fmax(tm, sm[k]);
+            tb |= sb[k];
+        }
+        part[3 * blockIdx.x] = ts;
+        part[3 * blockIdx.x + 1] = tm;
+        part[3 * blockIdx.x + 2] = (double)tb;
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__restrict__ part, int nb,
+                                                           double *__restrict__ out)
+{
+    __shared__ double ss[kRedThreads], sm[kRedThreads], sb[kRedThreads];
+    double s = 0.0, mx = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        s += part[3 * k];
+        mx = fmax(mx, part[3 * k + 1]);
+        b = fmax(b, part[3 * k + 2]);
+    }
+    ss[threadIdx.x] = s;
+    sm[threadIdx.x] = mx;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            ss[threadIdx.x] += ss[threadIdx.x + o];
+            sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+            sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = ss[0];
+        out[1] = sm[0];
+        out[2] = sb[0];
+    }
+}
+
+template <class R>
+void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long n, double *partials,
+                      double *out, cudaStream_t st)
+{
+    const int nb = diag_partial_blocks(n);
+    k_mass_partial<R><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, partials);
+    k_mass_final<<<1, kRedThreads, 0, st>>>(partials, nb, out);
+}
+
+// --------------------------------------------------------- contact angle ----
+// One block.  Warp w < 8 searches row k = 2 + w/2 for the left (w even) or
+// right (w odd) mid-density crossing; the reference scans left-to-right
+// (right-to-left) and stops at the first hit, i.e. the minimum (maximum)
+// index satisfying the crossing test, found here by a warp min (max).
+// Warp 8 then finds the top of the cap on the centre column (the reference
+// keeps the last hit, the maximum k).  Thread 0 does the extrapolation and
+// angle arithmetic in FP64 exactly as the reference.
+template <class R>
+__global__ void k_contact_angle(const R *__restrict__ rho, int dx, int dy, int dz, int tier,
+                                double mid, double *__restrict__ out)
+{
+    __shared__ double px[8];
+    __shared__ int ic_s;
+    __shared__ double H_s;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    auto T = [&](int i, int k) -> double { return (double)rho[((long long)i * dy + tier) * dz + k]; };
+    if (w < 8) {
+        const int row = 2 + w / 2;
+        if ((w & 1) == 0) {
+            int best = INT_MAX;
+            for (int i = l; i < dx / 2 + 2; i += 32) {
+                const double t1 = T(i + 1, row), t2 = T(i + 2, row);
+                if (t1 < mid && t2 >= mid) best = min(best, i);
+            }
+            best = warp_min_i(best);
+            if (l == 0) {
+                double v = 0.0;
+                if (best != INT_MAX) {
+                    const double t1 = T(best + 1, row), t2 = T(best + 2, row);
+                    v = (double)(best + 1) + (t1 - mid) / (t1 - t2);
+                }
+                px[w] = v;
+            }
+        } else {
+            int best = INT_MIN;
+            for (int i = dx - 2 - l; i > dx / 2 - 2; i -= 32) {
+                const double t1 = T(i - 1, row), t2 = T(i - 2, row);
+                if (t1 < mid && t2 >= mid) best = max(best, i);
+            }
+            best = warp_max_i(best);
+            if (l == 0) {
+                double v = 0.0;
+                if (best != INT_MIN) {
+                    const double t1 = T(best - 1, row), t2 = T(best - 2, row);
+                    v = (double)(best - 1) - (t1 - mid) / (t1 - t2);
+                }
+                px[w] = v;
+            }
+        }
+    }
+    __syncthreads();
+    const bool have = px[0] != 0.0 && px[1] != 0.0;
+    if (threadIdx.x == 0) ic_s = (int)((px[4] + px[5]) / 2 + 0.5);
+    __syncthreads();
+    if (w == 8) {
+        int best = INT_MIN;
+        const int ic = ic_s;
+        if (have && ic >= 0 && ic < dx) {
+            for (int k = 2 + l; k < dz - 2; k += 32) {
+                const double t = T(ic, k), t1 = T(ic, k + 1);
+                if (t >= mid && t1 < mid) best = max(best, k);
+            }
+        }
+        best = warp_max_i(best);
+        if (l == 0) {
+            double H = 0.0;
+            if (best != INT_MIN) {
+                const double t = T(ic, best), t1 = T(ic, best + 1);
+                H = (double)best + (t - mid) / (t - t1) - 2.0;
+            }
+            H_s = H;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double PI = 3.14159265358979323846264338327950288;
+    const double y0 = 2, y1 = 3, y2 = 4;
+    double xl, xr, cl, cr, cap = 0.0, H = 0.0, L = 0.0;
+    if (have) {
+        xl = px[2] * ((y0 - y2) / (y1 - y2)) + px[4] * ((y0 - y1) / (y2 - y1));
+        xr = px[3] * ((y0 - y2) / (y1 - y2)) + px[5] * ((y0 - y1) / (y2 - y1));
+        double ca = atan((y1 - y0) / (px[2] - xl));
+        if (ca < 0) ca += PI;
+        cl = ca / PI * 180;
+        ca = atan(-(y1 - y0) / (px[3] - xr));
+        if (ca < 0) ca += PI;
+        cr = ca / PI * 180;
+        L = xr - xl;
+        H = H_s;
+        if (L <= 0) {
+            L = px[3] - px[2];
+            H = H - 0.5;
+        }
+        if (xl > dy / 2 && xr < dy / 2) {
+            xl = dy / 2;
+            xr = dy / 2;
+        }
+        const double Rr = (H * H * 4 + L * L) / H / 8;
+        cap = atan(L / (Rr - H) / 2);
+        if (cap < 0) cap += PI;
+        cap = cap / PI * 180;
+    } else {
+        xl = xr = dy / 2;
+        cl = cr = 0;
+    }
+    out[0] = cl;
+    out[1] = cr;
+    out[2] = cap;
+    out[3] = xl;
+    out[4] = xr;
+    out[5] = H;
+    out[6] = L;
+}
+
+template <class R>
+void diag_launch_contact_angle(const R *rho, int dx, int dy, int dz, int tier, double den_g,
+                               double den_l, double *out, cudaStream_t st)
+{
+    k_contact_angle<R><<<1, 288, 0, st>>>(rho, dx, dy, dz, tier, (den_g + den_l) / 2, out);
+}
+
+// ------------------------------------------------------------ Laplace ----
+__device__ double eos_pressure(int eos, double A, double B, double T, double r)
+{
+    if (eos == 1) return T * r / (1.0 - B * r) - A * r * r;
+    if (eos == 2) {
+        const double e = B * r, om = 1.0 - e;
+        return r * T * (1 + e + e * e - e * e * e) / (om * om * om) - A * r * r;
+    }
+    if (eos == 3) return T * r / (1.0 - B * r) - A * r * r / (1.0 + B * r);
+    return T * r / (1.0 - B * r) - A * r * r / (1.0 + B * r * 2 - (B * r) * (B * r));
+}
+
+template <class R>
+__global__ void k_laplace(const R *__restrict__ rho, int dx, int dy, int dz, int eos, double A,
+                          double B, double T, double kk, double *__restrict__ out)
+{
+    const int l = threadIdx.x;
+    auto D = [&](int j) -> double { return (double)rho[((long long)(dx / 2) * dy + j) * dz + dz / 2]; };
+    const double tout = D(0), tin = D(dy / 2);
+    const double mid = (tout + tin) / 2;
+    int best = INT_MAX;
+    for (int j = l; j <= dy / 2 && j + 1 < dy; j += 32) {
+        const double t1 = D(j), t2 = D(j + 1);
+        if (t1 <= mid && t2 > mid) best = min(best, j);
+    }
+    best = warp_min_i(best);
+    if (l != 0) return;
+    double Rr = 0.0;
+    if (best != INT_MAX) {
+        const double t1 = D(best), t2 = D(best + 1);
+        const double pos = (double)best + (mid - t1) / (t2 - t1);
+        Rr = (double)(dy / 2) - pos;
+    }
+    const double dp = eos_pressure(eos, A, B, T, tin) - eos_pressure(eos, A, B, T, tout);
+    out[0] = Rr;
+    out[1] = dp;
+    out[2] = kk * dp * Rr / 2;
+}
+
+template <class R>
+void diag_launch_laplace(const R *rho, int dx, int dy, int dz, int eos, double A, double B, double T,
+                         double kk, double *out, cudaStream_t st)
+{
+    k_laplace<R><<<1, 32, 0, st>>>(rho, dx, dy, dz, eos, A, B, T, kk, out);
+}
+
+__global__ void k_mv(const uint8_t *type, const float *rho, const float *u, const float *F, float *mv,
+                     long long n)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= n || type[I] != FLUID) return;
+    const float r = rho[I];
+    for (int a = 0; a < 3; ++a) mv[I + a * n] = u[I + a * n] + F[I + a * n] / r * 0.5f;
+}
+
+void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const float *F, float *mv,
+                    long long n, cudaStream_t st)
+{
+    k_mv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(type, rho, u, F, mv, n);
+}
+
+template void diag_launch_mass<float>(const uint8_t *, const float *, const float *, long long, double *, double *, cudaStream_t);
+template void diag_launch_mass<double>(const uint8_t *, const double *, const double *, long long, double *, double *, cudaStream_t);
+template void diag_launch_contact_angle<float>(const float *, int, int, int, int, double, double, double *, cudaStream_t);
+template void diag_launch_contact_angle<double>(const double *, int, int, int, int, double, double, double *, cudaStream_t);
+template void diag_launch_laplace<float>(const float *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
+template void diag_launch_laplace<double>(const double *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
+
+}  // namespace cpmp

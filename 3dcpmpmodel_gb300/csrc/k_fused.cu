@@ -1,0 +1,248 @@
+// k_fused.cu -- FUSED scheme instantiations and launchers.
+#include "k_fused.cuh"
+#include "k_plain.cuh"  // k_wall_pass
+#include "kernels.h"
+#include "../../include/cpmp.h"
+
+namespace cpmp {
+
+__global__ void k_init_fused_a(KParams<float> p, DropletDev d, uint8_t *type, float *rho, float *f0)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= p.n) return;
+    const int k = (int)(I % p.dz), j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    if (solid_k(p.wall_mode, k, p.dz)) {
+        type[I] = SOLID;
+        const float w = p.wall[(k < 3 ? 0 : (long long)p.dx * p.dy) + (long long)i * p.dy + j];
+        rho[I] = w;
+        f0[I] = w * wgt<float>(0);
+    } else {
+        type[I] = FLUID;
+        const double r0 = droplet_density(d, i, j, k, p.dx, p.dy);
+        rho[I] = (float)r0;
+        f0[I] = (float)(r0 * wgt<double>(0));
+    }
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) k_decode(KParams<float> p, int P, const S *__restrict__ h,
+                                                const float *__restrict__ f0, void *dst, int as_f64)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= p.n) return;
+    const int k = (int)(I % p.dz);
+    if (solid_k(p.wall_mode, k, p.dz)) return;
+    const int j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    float f[Q];
+    gather_pops<S>(p, P, h, f0, i, j, k, I, f);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (as_f64)
+            ((double *)dst)[q * p.n + I] = f[q];
+        else
+            ((float *)dst)[q * p.n + I] = f[q];
+    }
+}
+
+// Encode natural-order populations: rest populations first (anchors) ...
+__global__ void k_encode_a(KParams<float> p, float *f0, const void *src, int as_f64)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= p.n) return;
+    if (solid_k(p.wall_mode, (int)(I % p.dz), p.dz)) return;
+    f0[I] = as_f64 ? (float)((const double *)src)[I] : ((const float *)src)[I];
+}
+// ... then the moving populations into the slots parity P reads them from.
+template <class S>
+__global__ void k_encode_b(KParams<float> p, int P, S *h, const float *f0, const void *src, int as_f64)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= p.n) return;
+    const int k = (int)(I % p.dz);
+    if (solid_k(p.wall_mode, k, p.dz)) return;
+    const int j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    for (int q = 1; q < Q; ++q) {
+        const float fq = as_f64 ? (float)((const double *)src)[q * p.n + I] : ((const float *)src)[q * p.n + I];
+        const int si = wrap1(i - cx(q), p.dx), sj = wrap1(j - cy(q), p.dy), sk = wrap1(k - cz(q), p.dz);
+        const bool ss = solid_k(p.wall_mode, sk, p.dz);
+        const long long s = ((long long)si * p.dy + sj) * p.dz + sk;
+        const float a = ss ? f0[I] : f0[s];
+        const S hv = f2s<S>((fq - ratio0(q) * a) * inv_w(q));
+        if (P == 0 || ss)
+            h[(long long)(q - 1) * p.n + I] = hv;
+        else
+            h[(long long)(opp(q) - 1) * p.n + s] = hv;
+    }
+}
+
+template <class S>
+__global__ void __launch_bounds__(256) k_velocity(KParams<float> p, int P, const S *__restrict__ h,
+                                                  const float *__restrict__ f0, const float *__restrict__ rho,
+                                                  float *__restrict__ u)
+{
+    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= p.n) return;
+    const int k = (int)(I % p.dz);
+    if (solid_k(p.wall_mode, k, p.dz)) return;
+    const int j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    float f[Q];
+    gather_pops<S>(p, P, h, f0, i, j, k, I, f);
+    const float r = rho[I];
+    u[I] = (f[1] + f[7] + f[9] + f[11] + f[13] - f[2] - f[8] - f[10] - f[12] - f[14]) / r;
+    u[I + p.n] = (f[3] + f[7] + f[8] + f[15] + f[17] - f[4] - f[9] - f[10] - f[16] - f[18]) / r;
+    u[I + 2 * p.n] = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) / r;
+}
+
+// ------------------------------------------------------------- dispatch ----
+namespace {
+constexpr int kTiles[][2] = {{4, 32}, {8, 32}, {2, 64}, {1, 128}};
+constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
+
+template <class F>
+void with_storage(int storage, F &&f)
+{
+    if (storage == CPMP_STORE_F16)
+        f(__half{});
+    else if (storage == CPMP_STORE_BF16)
+        f(__nv_bfloat16{});
+    else
+        f(float{});
+}
+
+template <class S, int TY, int TZ, int L>
+void launch_collide_t(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
+                      float *f0n, const float *rho, cudaStream_t st)
+{
+    const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + t.xl - 1) / t.xl);
+    k_fused_collide<S, TY, TZ, L><<<grid, TY * TZ, fused_smem_bytes<TY, TZ, L>(), st>>>(p, P, h, f0c, f0n, rho, t.xl);
+}
+
+template <class S, int L>
+void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
+                      float *f0n, const float *rho, cudaStream_t st)
+{
+    if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, st);
+    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, st);
+}
+
+template <class S, int TY, int TZ, int L>
+cudaError_t set_attr_t()
+{
+    return cudaFuncSetAttribute(k_fused_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fused_smem_bytes<TY, TZ, L>());
+}
+template <class S, int L>
+cudaError_t set_attr_l()
+{
+    cudaError_t e;
+    if ((e = set_attr_t<S, 4, 32, L>()) != cudaSuccess) return e;
+    if ((e = set_attr_t<S, 8, 32, L>()) != cudaSuccess) return e;
+    if ((e = set_attr_t<S, 2, 64, L>()) != cudaSuccess) return e;
+    return set_attr_t<S, 1, 128, L>();
+}
+}  // namespace
+
+int fused_tile_count() { return kNumTiles; }
+FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl}; }
+bool fused_tile_supported(int ty, int tz)
+{
+    for (int i = 0; i < kNumTiles; ++i)
+        if (kTiles[i][0] == ty && kTiles[i][1] == tz) return true;
+    return false;
+}
+
+cudaError_t fused_setup_attributes()
+{
+    cudaError_t e;
+    if ((e = set_attr_l<__half, 2>()) != cudaSuccess) return e;
+    if ((e = set_attr_l<__half, 3>()) != cudaSuccess) return e;
+    if ((e = set_attr_l<__nv_bfloat16, 2>()) != cudaSuccess) return e;
+    if ((e = set_attr_l<__nv_bfloat16, 3>()) != cudaSuccess) return e;
+    if ((e = set_attr_l<float, 2>()) != cudaSuccess) return e;
+    return set_attr_l<float, 3>();
+}
+
+void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
+                       float *rho, float *f0, void *h, cudaStream_t st)
+{
+    const unsigned g = (unsigned)((p.n + 255) / 256);
+    k_init_fused_a<<<g, 256, 0, st>>>(p, d, type, rho, f0);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_init_fused_b<S><<<g, 256, 0, st>>>(p, rho, f0, (S *)h);
+    });
+}
+
+void fused_launch_wall(const KParams<float> &p, float *rho, cudaStream_t st, LaunchHook *hook)
+{
+    if (p.wall_mode != 1) return;
+    const long long np = (long long)p.dx * p.dy;
+    const unsigned gw = (unsigned)((np + 127) / 128);
+    for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) {
+        hook_begin(hook, K_WALL, st);
+        k_wall_pass<float><<<gw, 128, 0, st>>>(p, s, rho, nullptr);
+        hook_end(hook, K_WALL, st);
+    }
+}
+
+void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
+                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
+                          LaunchHook *hook)
+{
+    hook_begin(hook, K_FUSED, st);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        if (p.lap_order == 7)
+            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, st);
+        else
+            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, st);
+    });
+    hook_end(hook, K_FUSED, st);
+}
+
+void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
+                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook)
+{
+    const unsigned g = (unsigned)((p.n + 255) / 256);
+    hook_begin(hook, K_DENSITY, st);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_density<S><<<g, 256, 0, st>>>(p, P, (const S *)h, f0, rho);
+    });
+    hook_end(hook, K_DENSITY, st);
+}
+
+void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,
+                         void *dst, bool dst_is_f64, cudaStream_t st)
+{
+    const unsigned g = (unsigned)((p.n + 255) / 256);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_decode<S><<<g, 256, 0, st>>>(p, P, (const S *)h, f0, dst, dst_is_f64 ? 1 : 0);
+    });
+}
+
+void fused_launch_encode(int storage, const KParams<float> &p, int P, void *h, float *f0,
+                         const void *src, bool src_is_f64, cudaStream_t st)
+{
+    const unsigned g = (unsigned)((p.n + 255) / 256);
+    k_encode_a<<<g, 256, 0, st>>>(p, f0, src, src_is_f64 ? 1 : 0);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_encode_b<S><<<g, 256, 0, st>>>(p, P, (S *)h, f0, src, src_is_f64 ? 1 : 0);
+    });
+}
+
+void fused_launch_velocity(int storage, const KParams<float> &p, int P, const void *h,
+                           const float *f0, const float *rho, float *u, cudaStream_t st)
+{
+    const unsigned g = (unsigned)((p.n + 255) / 256);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_velocity<S><<<g, 256, 0, st>>>(p, P, (const S *)h, f0, rho, u);
+    });
+}
+
+}  // namespace cpmp

@@ -1,0 +1,9 @@
+// PLAIN scheme, FP32 storage and arithmetic (default FMA contraction).
+#include "k_plain.cuh"
+
+namespace cpmp {
+template void plain_launch_init<float, float>(const KParams<float> &, const DropletDev &, uint8_t *, float *, float *, float *, float *, cudaStream_t);
+template void plain_launch_step<float, float>(const KParams<float> &, const uint8_t *, float *, float *, float *, float *, float *, const float *, float *, cudaStream_t, LaunchHook *);
+template void plain_launch_macro<float, float>(const KParams<float> &, const uint8_t *, const float *, float *, float *, cudaStream_t);
+template void plain_launch_mu_force<float>(const KParams<float> &, const uint8_t *, float *, float *, float *, cudaStream_t);
+}  // namespace cpmp

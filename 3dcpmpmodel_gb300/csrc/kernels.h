@@ -1,0 +1,93 @@
+// kernels.h -- host-side declarations of every kernel launcher.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "launch.h"
+#include "lbm_core.cuh"
+
+namespace cpmp {
+
+// ---- PLAIN scheme (k_plain_f32.cu, k_plain_f64.cu) ------------------------
+template <class R, class S>
+void plain_launch_init(const KParams<R> &p, const DropletDev &d, uint8_t *type, R *rho, R *mu, R *u,
+                       S *f, cudaStream_t st);
+template <class R, class S>
+void plain_launch_step(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *u, R *F, R *mv,
+                       const S *fc, S *fn, cudaStream_t st, LaunchHook *hook);
+template <class R, class S>
+void plain_launch_macro(const KParams<R> &p, const uint8_t *type, const S *f, R *rho, R *u,
+                        cudaStream_t st);
+template <class R>
+void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
+                           cudaStream_t st);
+
+extern template void plain_launch_init<float, float>(const KParams<float> &, const DropletDev &, uint8_t *, float *, float *, float *, float *, cudaStream_t);
+extern template void plain_launch_step<float, float>(const KParams<float> &, const uint8_t *, float *, float *, float *, float *, float *, const float *, float *, cudaStream_t, LaunchHook *);
+extern template void plain_launch_macro<float, float>(const KParams<float> &, const uint8_t *, const float *, float *, float *, cudaStream_t);
+extern template void plain_launch_mu_force<float>(const KParams<float> &, const uint8_t *, float *, float *, float *, cudaStream_t);
+extern template void plain_launch_init<double, double>(const KParams<double> &, const DropletDev &, uint8_t *, double *, double *, double *, double *, cudaStream_t);
+extern template void plain_launch_step<double, double>(const KParams<double> &, const uint8_t *, double *, double *, double *, double *, double *, const double *, double *, cudaStream_t, LaunchHook *);
+extern template void plain_launch_macro<double, double>(const KParams<double> &, const uint8_t *, const double *, double *, double *, cudaStream_t);
+extern template void plain_launch_mu_force<double>(const KParams<double> &, const uint8_t *, double *, double *, double *, cudaStream_t);
+
+// ---- FUSED scheme (k_fused.cu) --------------------------------------------
+// storage: CPMP_STORE_F32 / F16 / BF16
+struct FusedTile {
+    int ty, tz, xl;
+};
+// Tile shapes instantiated for the fused kernel; the autotuner picks among
+// them per grid.
+int fused_tile_count();
+FusedTile fused_tile(int idx, int xl);
+bool fused_tile_supported(int ty, int tz);
+
+cudaError_t fused_setup_attributes();
+void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
+                       float *rho, float *f0, void *h, cudaStream_t st);
+void fused_launch_wall(const KParams<float> &p, float *rho, cudaStream_t st, LaunchHook *hook);
+void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
+                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
+                          LaunchHook *hook);
+void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
+                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook);
+// Natural-order populations (post-stream at each node) to/from device
+// buffers of FP32 or FP64 (dst_is_f64).
+void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,
+                         void *dst, bool dst_is_f64, cudaStream_t st);
+void fused_launch_encode(int storage, const KParams<float> &p, int P, void *h, float *f0,
+                         const void *src, bool src_is_f64, cudaStream_t st);
+// Bare velocity of the current state.
+void fused_launch_velocity(int storage, const KParams<float> &p, int P, const void *h,
+                           const float *f0, const float *rho, float *u, cudaStream_t st);
+
+// ---- diagnostics (k_diag.cu) ----------------------------------------------
+// Deterministic FP64 reduction: out[0] = sum rho (fluid), out[1] = max |mv|^2,
+// out[2] = non-finite flag.  `partials` holds 3 * diag_partial_blocks(n)
+// doubles.
+int diag_partial_blocks(long long n);
+template <class R>
+void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long n, double *partials,
+                      double *out, cudaStream_t st);
+// Contact angle on the x-z slice j = tier: out[7] = CaLeft, CaRight, CaCap,
+// XLeft, XRight, H, L (ContactAngle, FluidCuda.cu:557-734).
+template <class R>
+void diag_launch_contact_angle(const R *rho, int dx, int dy, int dz, int tier, double den_g,
+                               double den_l, double *out, cudaStream_t st);
+// Laplace probe along y through (DX/2, ., DZ/2): out[3] = R, dp, sigma.
+template <class R>
+void diag_launch_laplace(const R *rho, int dx, int dy, int dz, int eos, double A, double B, double T,
+                         double kk, double *out, cudaStream_t st);
+// mv = u + F / (2 rho) on fluid nodes.
+void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const float *F, float *mv,
+                    long long n, cudaStream_t st);
+
+extern template void diag_launch_mass<float>(const uint8_t *, const float *, const float *, long long, double *, double *, cudaStream_t);
+extern template void diag_launch_mass<double>(const uint8_t *, const double *, const double *, long long, double *, double *, cudaStream_t);
+extern template void diag_launch_contact_angle<float>(const float *, int, int, int, int, double, double, double *, cudaStream_t);
+extern template void diag_launch_contact_angle<double>(const double *, int, int, int, int, double, double, double *, cudaStream_t);
+extern template void diag_launch_laplace<float>(const float *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
+extern template void diag_launch_laplace<double>(const double *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
+
+}  // namespace cpmp

@@ -1,0 +1,394 @@
+"""Benchmark: MLUPS of the chemical-potential multiphase D3Q19 MRT step.
+
+Default workload (N=1): the 512^3 precision configuration -- RKS EOS at
+T/Tc = 0.75, z walls, droplet radius 100, FUSED scheme with FP16 population
+storage (the headline configuration; its 5.9 GB state is far larger than
+the 129 MB L2, so no L2 flush is needed between steps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c3|c2|c1] [--storage f16|bf16|f32] [--scheme fused|plain]
+
+Under torchrun (N > 1) every rank runs an independent replica (the step does
+not shard on one GPU per box); value is the sum over ranks, time the max.
+``--impl reference`` times the reference's own kernels compiled for the host
+(oracle/_ref, FP64, OpenMP over every host core) -- or the FP64 oracle port
+when that build is absent -- on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS (lattice updates/s / 1e6), FP16-storage fused step"
+Q = 19
+
+WORKLOADS = {
+    # configs of the benchmark set; sizes and physics as stated
+    "c3": dict(name="precision_512cube_rks_fp16", dx=512, dy=512, dz=512, model=205, tr=0.75,
+               radius=100.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8),
+    "c2": dict(name="wetting_128x128x96_prw", dx=128, dy=128, dz=96, model=202, tr=0.7,
+               radius=30.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8,
+               centre=(64.0, 64.0, 3.0)),
+    "c1": dict(name="periodic_64cube_cs", dx=64, dy=64, dz=64, model=206, tr=0.85, eos_a=0.5,
+               eos_b=4.0, radius=16.0, width=2.0, wall_mode=0, base_pt=0.0, k=0.2, ka=0.01,
+               tau=1.0, centre=(32.0, 32.0, 32.0)),
+}
+
+
+def storage_bytes(storage: str) -> int:
+    return {"f16": 2, "bf16": 2, "f32": 4, "f64": 8}[storage]
+
+
+def algorithmic_bytes(scheme: str, storage: str) -> dict:
+    """Algorithmic bytes per lattice update.
+
+    B_LU = 2*19*s + 8 is the step-level unit (every population read and
+    written once, one FP32 density written and read once).  Per kernel of the
+    FUSED scheme: the fused collide reads and writes 18 moving populations of
+    s bytes plus the FP32 rest population, and reads the density (4 B);
+    the density pass reads the populations and writes the density."""
+    s = storage_bytes(storage)
+    b_lu = 2 * Q * s + 8
+    if scheme == "fused":
+        return {"step": b_lu, "fused_collide": 2 * (18 * s + 4) + 4, "density": 18 * s + 4 + 4}
+    r = 8 if storage == "f64" else 4
+    return {"step": b_lu, "collide_stream": 2 * Q * r + 12 * r + 1, "macro": Q * r + 4 * r + 1}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_solver(cp, wl: dict, scheme: str, storage: str, device: int):
+    kw = {k: v for k, v in wl.items() if k not in ("name", "radius", "width", "centre")}
+    s = cp.Solver(scheme=cp.SCHEME[scheme], storage=cp.STORE[storage], device=device, **kw)
+    s.set_flow_field(radius=wl["radius"], width=wl["width"], centre=wl.get("centre"))
+    return s
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_ours(args) -> None:
+    import importlib
+
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    importlib.import_module("3dcpmpmodel_gb300.build").build()
+    cp = importlib.import_module("3dcpmpmodel_gb300")
+    wl = WORKLOADS[args.workload]
+    s = make_solver(cp, wl, args.scheme, args.storage, local)
+    n = s.n
+    stream = torch.cuda.ExternalStream(s.stream)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up (includes graph capture)
+    s.step(args.warmup)
+    s.sync()
+    # ---- timed region: device-resident state, CUDA events on the solver's stream
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    l0 = s.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    s.sync()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    launches = s.launch_count - l0
+    ms_max = ms
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    mlups_rank = n * args.steps / (ms_max / 1e3) / 1e6
+    value = mlups_rank * ws
+
+    # ---- per-kernel timing pass (same workload, events around each launch)
+    s.kernel_timing(True)
+    s.step(args.steps)
+    s.sync()
+    kt = s.kernel_times()
+    s.kernel_timing(False)
+    bytes_per = algorithmic_bytes(args.scheme, args.storage)
+    dom = max(kt.items(), key=lambda kv: kv[1][1])
+    dom_name, (dom_launches, dom_ms) = dom
+    per_launch_s = dom_ms / dom_launches / 1e3
+    units_per_launch = n  # one launch updates every node once
+    alg = bytes_per.get(dom_name, bytes_per["step"])
+    achieved = alg * units_per_launch / per_launch_s / 1e9
+    peaks = measured_peaks()
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"{dom_name}_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        key = f"{args.workload}_{args.storage}"
+        if key in tj:
+            traffic = tj[key]
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": round(achieved / peaks["hbm_gbs"], 4),
+                "peak_source": peaks["source"], "traffic": traffic,
+                "alg_bytes_per_lu": alg,
+                "kernels_ms_per_step": {k: round(v[1] / max(1, v[0]) * (v[0] / args.steps), 4)
+                                        for k, v in kt.items()}}
+
+    # ---- end to end through the public API with host buffers:
+    # upload a state (DIST, FP32, pinned host) -> K x (step + device
+    # diagnostics read back) -> density read back to pinned host.
+    e2e = None
+    if not args.no_e2e:
+        host_f = torch.empty(Q * n, dtype=torch.float32, pin_memory=True).numpy()
+        host_r = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        cpl = cp.lib()
+        import ctypes as C
+        cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
+                                         host_f.ctypes.data_as(C.c_void_p), C.c_size_t(host_f.nbytes)))
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        cp._abi.check(cpl.cpmp_set_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
+                                         host_f.ctypes.data_as(C.c_void_p), C.c_size_t(host_f.nbytes)))
+        diag = cp.Diag()
+        for _ in range(args.steps):
+            cp._abi.check(cpl.cpmp_step(s._h, 1))
+            rc = cpl.cpmp_reduce(s._h, C.byref(diag))
+            if rc not in (0, cp._abi.CPMP_ERR_NONFINITE):
+                cp._abi.check(rc)
+        cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["rho"], cp._abi.CPMP_F32,
+                                         host_r.ctypes.data_as(C.c_void_p), C.c_size_t(host_r.nbytes)))
+        t1 = time.perf_counter()
+        dt = t1 - t0
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([dt], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": round(n * args.steps / dt / 1e6 * ws, 1), "unit": "MLUPS",
+               "h2d_bytes_per_step": int(host_f.nbytes / args.steps),
+               "d2h_bytes_per_step": int((host_r.nbytes + args.steps * C.sizeof(cp.Diag)) / args.steps),
+               "what": "cpmp_set_field(DIST, pinned FP32) + K x (cpmp_step(1) + cpmp_reduce) + "
+                       "cpmp_get_field(RHO, pinned FP32)"}
+
+    # ---- CPU baseline on rank 0 (bounded sample)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(args, wl)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 arithmetic, " + args.storage + " population storage",
+            "data": "synthetic (seeded droplet initial field, no dataset)",
+            "config": {"workload": wl["name"], "grid": [wl["dx"], wl["dy"], wl["dz"]],
+                       "scheme": args.scheme, "storage": args.storage, "model": wl["model"],
+                       "tr": wl["tr"], "tile": None, "parallelism": f"replicas{ws}",
+                       "l2": "state larger than L2 (no flush needed)" if n * 44 > 129e6
+                             else "state fits in L2; numbers are L2-resident"},
+            "gpu_launches": launches, "clocks": clk, "roofline": roofline, "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    s.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_sample(args, wl: dict) -> dict:
+    """The reference's kernels on the host cores (oracle/_ref, FP64, OpenMP),
+    or the oracle port, over a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    kind = "reference"
+    try:
+        if O.build_ref() is None:
+            kind = "port"
+    except Exception:
+        kind = "port"
+    if wl["wall_mode"] != 1:
+        kind = "port"  # the reference step always has z walls
+    # bounded sample: same physics, grid capped so a step takes seconds
+    dx, dy, dz = wl["dx"], wl["dy"], wl["dz"]
+    cap = args.cpu_nodes
+    while dx * dy * dz > cap:
+        if dx >= dy and dx >= dz:
+            dx //= 2
+        elif dy >= dz:
+            dy //= 2
+        else:
+            dz //= 2
+    model = wl["model"]
+    tr = wl["tr"]
+    kw = dict(dx=dx, dy=dy, dz=dz, model=model, tr=tr, K=wl["k"], Ka=wl["ka"], tau=wl["tau"],
+              base_pt=wl["base_pt"], radius=min(wl["radius"], dz / 3), width=wl["width"],
+              wall_mode=wl["wall_mode"])
+    if "eos_a" in wl:
+        kw["eos_a"], kw["eos_b"] = wl["eos_a"], wl["eos_b"]
+    if wl.get("centre") is not None:
+        kw["centre"] = (dx / 2, dy / 2, min(wl["centre"][2], dz / 2))
+    s = O.Setup(**kw)
+    g, l = O.coexistence(model, tr, s.eos_a, s.eos_b)
+    st = O.State(s, g, l, "ref" if kind == "reference" else "oracle").init()
+    st.step(1)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        st.step(1)
+        steps += 1
+        if time.perf_counter() - t0 > args.cpu_seconds:
+            break
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": round(dx * dy * dz * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": cores,
+            "kind": kind, "sample": f"{steps} steps of a {dx}x{dy}x{dz} box, same EOS/T/walls, FP64"}
+
+
+def run_reference(args) -> None:
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.workload]
+    for _ in range(args.warmup):
+        pass
+    samples = []
+    cpu = None
+    for _ in range(max(1, min(args.steps, args.ref_repeats))):
+        cpu = cpu_sample(args, wl)
+        samples.append(cpu["value"])
+    v = statistics.median(samples)
+    cpu["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded droplet initial field, no dataset)",
+            "config": {"workload": wl["name"], "grid": [wl["dx"], wl["dy"], wl["dz"]],
+                       "parallelism": "host cores"},
+            "impl": "reference", "cpu_baseline": cpu,
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c3")
+    ap.add_argument("--scheme", choices=["fused", "plain"], default="fused")
+    ap.add_argument("--storage", choices=["f16", "bf16", "f32", "f64"], default="f16")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-nodes", type=int, default=2_000_000)
+    ap.add_argument("--ref-repeats", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+/*
+ * cpmp.h -- C ABI of the GB300 chemical-potential multiphase D3Q19 MRT
+ * lattice-Boltzmann step.
+ *
+ * The reference (zhou-yiling/3DCPMPmodel) has no library interface: its step
+ * contract is a set of global device fields, __constant__ parameters, a
+ * compile-time grid and a per-step launch sequence inside main().  Each entry
+ * point below replaces one piece of that contract; the comment on each names
+ * the reference code it stands in for (file:line in the reference tree).
+ *
+ * Conventions
+ *   - The handle owns all device memory; host buffers are caller-owned.
+ *   - Every call returns a cpmp_status and never aborts or traps;
+ *     cpmp_last_error() gives a one-line message for the calling thread.
+ *   - One handle is used from one host thread at a time.
+ *   - Field layout is the reference's: node index I = (i*DY + j)*DZ + k
+ *     (z fastest, Common.h:164); vector fields are three consecutive blocks
+ *     of N values (x, y, z); populations are 19 consecutive blocks of N.
+ */
+#ifndef CPMP_H
+#define CPMP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPMP_Q 19
+#define CPMP_ABI_VERSION 1
+
+typedef enum cpmp_status {
+    CPMP_OK = 0,
+    CPMP_ERR_PARAM = 1,       /* invalid argument or parameter set */
+    CPMP_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    CPMP_ERR_NOMEM = 3,       /* device or host allocation failed */
+    CPMP_ERR_COCURVE = 4,     /* coexistence table missing or T/Tc row absent */
+    CPMP_ERR_NONFINITE = 5,   /* NaN or negative density seen by cpmp_reduce */
+    CPMP_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    CPMP_ERR_UNSUPPORTED = 7, /* option combination not provided */
+    CPMP_ERR_SIZE = 8         /* buffer size does not match the field */
+} cpmp_status;
+
+/* Model ids of the chemical-potential family, reference Common.h:54-59. */
+enum {
+    CPMP_MP_CPVDW = 201,
+    CPMP_MP_CPPRW = 202,
+    CPMP_MP_CPPRM = 203,
+    CPMP_MP_CPRKE = 204,
+    CPMP_MP_CPRKS = 205,
+    CPMP_MP_CPCSE = 206
+};
+
+enum { CPMP_WALL_NONE = 0, CPMP_WALL_Z = 1 };
+enum { CPMP_STORE_F64 = 0, CPMP_STORE_F32 = 1, CPMP_STORE_F16 = 2, CPMP_STORE_BF16 = 3 };
+/* PLAIN: one kernel per reference kernel, two population lattices, reference
+ *        launch order (FluidCuda.cu:1279-1291); storage F64 or F32.
+ * FUSED: wall + fused mu/force/MRT/forcing/stream kernel + density kernel,
+ *        one in-place A-A population lattice; storage F32, F16 or BF16. */
+enum { CPMP_SCHEME_PLAIN = 0, CPMP_SCHEME_FUSED = 1 };
+enum { CPMP_F64 = 0, CPMP_F32 = 1 }; /* host dtype of cpmp_get_field/cpmp_set_field */
+
+typedef enum cpmp_field {
+    CPMP_FIELD_RHO = 0,   /* density, N            (reference Dens) */
+    CPMP_FIELD_U = 1,     /* bare velocity, 3N     (reference Vx,Vy,Vz) */
+    CPMP_FIELD_MV = 2,    /* physical velocity u+F/(2 rho), 3N (MVx,MVy,MVz) */
+    CPMP_FIELD_MU = 3,    /* chemical potential, N (reference Pote) */
+    CPMP_FIELD_FORCE = 4, /* non-ideal force, 3N   (reference Fx,Fy,Fz) */
+    CPMP_FIELD_DIST = 5,  /* post-stream populations, 19N (reference Dist) */
+    CPMP_FIELD_TYPE = 6   /* node tags FLUID=1 / SOLID=2, N bytes (Type) */
+} cpmp_field;
+
+/* Every knob of the reference's Initialize() (FluidCuda.cu:119-163),
+ * SetMultiphase() (FluidCuda.cu:1314-1394), the compile-time grid
+ * (Common.h:25-27) and the compile-time switches (FluidCuda.cu:1-7). */
+typedef struct cpmp_params {
+    int dx, dy, dz;       /* grid (Common.h:25-27) */
+    int model;            /* CPMP_MP_* (Initialize: MModel) */
+    double tr;            /* T/Tc (Tr) */
+    double k;             /* EOS scale: mu = K^2 mu0 - ka lap(rho) (K) */
+    double ka;            /* kappa (Ka) */
+    double k1, k2;        /* pressure-tensor correction (K1, K2) */
+    double tau;           /* shear relaxation time (Tau) */
+    double ts[CPMP_Q];    /* MRT rates (Ts[]); used when ts_from_tau == 0 */
+    int ts_from_tau;      /* 1: the reference's rates built from tau (FluidCuda.cu:154-157) */
+    double base_pt;       /* wall chemical potential (BasePt) */
+    double eos_a, eos_b;  /* CS constants a, b (0: the reference's a=1, b=4) */
+    double eos_omega;     /* PR/RKS acentric factor (0: the model's own) */
+    double den_g, den_l;  /* > 0: coexistence densities given directly */
+    const char *cocurve_dir; /* directory of CoCurve_<EOS>_2.txt; NULL: built-in
+                                Maxwell construction */
+    int wall_mode;        /* CPMP_WALL_Z: three solid layers at each z end
+                             (CONTACTANGLE); CPMP_WALL_NONE: periodic box */
+    int lap_order;        /* 5: GradD5 (PTCALCFIVEPOINT), 7: GradD7 (PTCALCSEVENPOINT) */
+    int complex_bc;       /* 1: layered wall extrapolation (COMPLEXCHEMBOUNDARY),
+                             0: SIMPLECHEMBOUNDARY */
+    int storage;          /* CPMP_STORE_* */
+    int scheme;           /* CPMP_SCHEME_* */
+    int device;           /* CUDA device ordinal */
+} cpmp_params;
+
+/* Initial droplet, SetFlowField (FluidCuda.cu:199-241). */
+typedef struct cpmp_droplet {
+    double cx, cy, cz;    /* centre (ignored when ref_centre = 1) */
+    double radius;        /* Radius */
+    double width;         /* tanh width parameter (Width) */
+    int ref_centre;       /* 1: the reference's placement (DX/2, DY/2, R+2) and
+                             its single-precision radius (FluidCuda.cu:215) */
+} cpmp_droplet;
+
+/* Diagnostics of CalcMacroCPU (FluidCuda.cu:1626-1657), ContactAngle
+ * (FluidCuda.cu:557-734) and the Laplace-law probe of SaveDataOriDen
+ * (FluidCuda.cu:1159-1199). */
+typedef struct cpmp_diag {
+    double mass;          /* FP64 sum of rho over fluid nodes */
+    double max_speed;     /* max |MV| over fluid nodes */
+    int nonfinite;        /* 1 if any fluid density is NaN or negative */
+    double ca_left, ca_right, ca_cap; /* contact angles (degrees), slice j = DY/2 */
+    double x_left, x_right;           /* contact-line positions */
+    double cap_h, cap_l;              /* spherical-cap height and base */
+    double lap_r;         /* droplet radius from the mid-density crossing along y */
+    double lap_dp;        /* EOS pressure jump p(inside) - p(outside) */
+    double lap_sigma;     /* K^2 * dp * R / 2 */
+    long long step;       /* steps taken since cpmp_init_droplet */
+} cpmp_diag;
+
+typedef struct cpmp_handle cpmp_handle;
+
+/* Fills the reference's defaults: Initialize() + CONTACTANGLE, five-point
+ * Laplacian, complex wall (FluidCuda.cu:1-7, 119-163); grid 64^3, FP32
+ * storage, PLAIN scheme, device 0. */
+void cpmp_params_default(cpmp_params *p);
+
+/* Replaces SetMultiphase + CudaInitialize (FluidCuda.cu:1314-1437): derives
+ * A, B, Tc, Rc and T, resolves the coexistence densities, allocates every
+ * field on the device and uploads the parameters. */
+cpmp_status cpmp_create(const cpmp_params *p, cpmp_handle **out);
+
+/* Replaces CudaFree (FluidCuda.cu:1463-1485). */
+void cpmp_destroy(cpmp_handle *h);
+
+/* Replaces the SetFlowField launch (FluidCuda.cu:1262). */
+cpmp_status cpmp_init_droplet(cpmp_handle *h, const cpmp_droplet *d);
+
+/* Replaces cudaMemcpyToSymbol(_BasePt) in the BasePt sweep
+ * (FluidCuda.cu:1264-1268); resets every wall column to this value. */
+cpmp_status cpmp_set_base_pt(cpmp_handle *h, double base_pt);
+
+/* Spatially varying wall chemical potential: 2*DX*DY values, bottom wall
+ * (k < 3) then top wall (k > DZ-4), column index i*DY + j.  Generalises the
+ * scalar _BasePt of ChemBoundary (FluidCuda.cu:387). */
+cpmp_status cpmp_set_wall_field(cpmp_handle *h, const double *host, size_t count);
+
+/* Replaces nsteps iterations of the step loop body (FluidCuda.cu:1277-1292):
+ * ChemBoundary, ChemPotential, NonidealForce, GlobalCollide, swap,
+ * MacroCalculate.  Asynchronous on the handle's stream (launch errors are
+ * reported here, execution errors by the next synchronising call). */
+cpmp_status cpmp_step(cpmp_handle *h, int nsteps);
+
+/* Waits for the handle's stream. */
+cpmp_status cpmp_sync(cpmp_handle *h);
+
+/* Device-to-host copy of one field (replaces the host reads of unified
+ * memory, e.g. FluidCuda.cu:563, 1626-1657).  dtype CPMP_F64 or CPMP_F32
+ * (TYPE is always bytes); bytes must equal the field size exactly. */
+cpmp_status cpmp_get_field(cpmp_handle *h, cpmp_field f, int dtype, void *host_dst, size_t bytes);
+
+/* Host-to-device copy of RHO, U or DIST (seeded states for parity runs).
+ * Setting DIST also recomputes RHO and U from it on fluid nodes. */
+cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *host_src,
+                           size_t bytes);
+
+/* Device reductions: CalcMacroCPU (mass, max|MV|, non-finite flag),
+ * ContactAngle(0, DY/2) and the Laplace probe.  Returns CPMP_ERR_NONFINITE
+ * (with *out filled) when a fluid density is NaN or negative, the condition
+ * on which the reference stops (FluidCuda.cu:1632-1646). */
+cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out);
+
+/* Coexistence densities (lattice units) the handle resolved, and the EOS
+ * constants it derived (SetMultiphase, FluidCuda.cu:1318-1384). */
+cpmp_status cpmp_get_eos(cpmp_handle *h, double *den_g, double *den_l, double *A, double *B,
+                         double *T, double *Rc);
+
+/* Stand-alone SetMultiphase: EOS constants and coexistence densities for a
+ * model and T/Tc (cocurve_dir NULL: built-in Maxwell construction). */
+cpmp_status cpmp_coexistence(int model, double tr, double eos_a, double eos_b, double eos_omega,
+                             const char *cocurve_dir, double *den_g, double *den_l, double *A,
+                             double *B, double *Tc, double *Rc);
+
+/* The CUDA stream the handle launches on (cudaStream_t). */
+void *cpmp_stream(cpmp_handle *h);
+
+/* Per-kernel timing for roofline reporting: while enabled, every kernel
+ * launch of cpmp_step is bracketed by CUDA events on the handle's stream and
+ * its duration accumulated by kernel class.  cpmp_kernel_times returns, for
+ * up to `cap` classes, the class name, launch count and total milliseconds;
+ * the return value is the number of classes. */
+cpmp_status cpmp_set_kernel_timing(cpmp_handle *h, int on);
+int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, double *ms, int cap);
+
+/* Number of the library's own kernel launches issued so far by this handle. */
+long long cpmp_launch_count(cpmp_handle *h);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *cpmp_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPMP_H */

@@ -1,0 +1,88 @@
+"""Build recipe for oracle/_ref: the reference's kernels compiled for the host.
+
+TEST INFRASTRUCTURE ONLY.  Generates, into oracle/_ref/ (git-ignored):
+
+* ``Common_rt.h``: the reference's Common.h with the grid constants made
+  run-time ints.  The only lines changed are the five ``const int`` grid
+  declarations (Common.h:25-27 and :33-34); everything else is verbatim.
+* ``ref_kernels.inc``: FluidCuda.cu lines 115-116 (the GridIndex/LineIndex
+  launch-index macros) and 188-463 (the kernels), verbatim.
+
+and compiles ``oracle/ref_shim.cpp`` against them into ``oracle/_ref/libref.so``.
+
+Generation needs the reference tree (``--src``, default the mounted
+reference); compiling needs only the generated files, so a machine without
+the reference tree can still build the library from a copied ``_ref/``.
+"""
+import argparse
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+DEFAULT_SRC = "/root/reference"
+
+GRID_LINES = {  # Common.h line (1-based) -> expected declaration prefix
+    25: "const int DY",
+    26: "const int DX",
+    27: "const int DZ",
+    33: "const int DXYZ",
+    34: "const int DXY",
+}
+INDEX_FIRST, INDEX_LAST = 115, 116
+KERNEL_FIRST, KERNEL_LAST = 188, 463
+
+
+def generate(src: str) -> None:
+    os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(src, "Common.h"), encoding="latin-1") as f:
+        common = f.read().split("\n")
+    for ln, prefix in GRID_LINES.items():
+        line = common[ln - 1]
+        if not line.startswith(prefix):
+            raise RuntimeError(f"Common.h:{ln} is not the expected grid constant: {line!r}")
+        common[ln - 1] = re.sub(r"^const int", "int", line)
+    with open(os.path.join(OUT, "Common_rt.h"), "w", encoding="latin-1") as f:
+        f.write("\n".join(common))
+    with open(os.path.join(src, "FluidCuda.cu"), encoding="latin-1") as f:
+        lines = f.read().split("\n")
+    index = lines[INDEX_FIRST - 1:INDEX_LAST]
+    body = lines[KERNEL_FIRST - 1:KERNEL_LAST]
+    if not (index[0].startswith("#define GridIndex") and index[1].startswith("#define LineIndex")
+            and any("__global__ void ChemPotential" in l for l in body)):
+        raise RuntimeError("FluidCuda.cu layout differs from the expected one")
+    body = ["#ifndef GridIndex"] + index + ["#endif"] + body
+    with open(os.path.join(OUT, "ref_kernels.inc"), "w", encoding="latin-1") as f:
+        f.write("\n".join(body) + "\n")
+
+
+def compile_lib() -> str:
+    out = os.path.join(OUT, "libref.so")
+    cmd = [
+        "g++", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+        "-std=c++17", "-I", OUT, os.path.join(HERE, "ref_shim.cpp"), "-o", out,
+    ]
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def build(src: str = DEFAULT_SRC) -> str | None:
+    """Generate (when the reference tree exists) and compile; returns the .so
+    path, or None when neither the reference tree nor generated files exist."""
+    if os.path.isfile(os.path.join(src, "FluidCuda.cu")):
+        generate(src)
+    if not (os.path.isfile(os.path.join(OUT, "Common_rt.h"))
+            and os.path.isfile(os.path.join(OUT, "ref_kernels.inc"))):
+        return None
+    return compile_lib()
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--src", default=DEFAULT_SRC)
+    a = ap.parse_args()
+    p = build(a.src)
+    print(p if p else "reference sources unavailable; nothing built")
+    sys.exit(0)

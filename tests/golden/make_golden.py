@@ -1,0 +1,92 @@
+"""Generate the committed golden fixtures from the reference itself.
+
+Run in a container that has the reference tree (default /root/reference):
+
+    python tests/golden/make_golden.py [--src /root/reference]
+
+Writes into tests/golden/:
+  * cocurve_rows.json  -- rows of the reference's CoCurve_<EOS>_2.txt tables
+    at the temperatures the tests and benchmarks use (reduced units);
+  * ref_<case>.npz     -- initial state and the state after N steps produced
+    by the reference's own kernels (FluidCuda.cu:188-463) compiled for the
+    host by oracle/build_ref.py, for small grids.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+TRS = [0.6, 0.65, 0.7, 0.75, 0.8, 0.85, 0.9]
+
+# name: (Setup kwargs, steps)
+CASES = {
+    # reference defaults (CP-PRW, Tr 0.7, K 0.2, Ka 0.001, tau 0.8), 3-D box with walls
+    "prw_walls_complex5": (dict(dx=24, dy=6, dz=20, radius=6.0, width=4.0, base_pt=-0.04), 40),
+    # the committed reference grid is quasi-2-D (DY = 1)
+    "prw_quasi2d": (dict(dx=28, dy=1, dz=18, radius=7.0, width=4.0, base_pt=0.02), 40),
+    # SIMPLECHEMBOUNDARY
+    "prw_walls_simple5": (dict(dx=16, dy=8, dz=18, radius=5.0, width=4.0, complex_bc=0,
+                               base_pt=-0.06), 30),
+    # PTCALCSEVENPOINT
+    "prw_walls_complex7": (dict(dx=18, dy=7, dz=20, radius=5.0, width=4.0, lap_order=7,
+                                base_pt=0.0), 30),
+    # K1/K2 pressure-tensor term and the PRM model
+    "prm_k1k2": (dict(dx=16, dy=6, dz=18, radius=5.0, width=4.0, model=O.MP_CPPRM, K1=0.002,
+                      K2=-0.002, tau=1.0), 25),
+}
+
+
+def cocurve(src: str) -> dict:
+    out = {}
+    for model, tag in O.TAG_OF_MODEL.items():
+        rows = {}
+        for tr in TRS:
+            r = O.read_cocurve(os.path.join(src, "CoCurve", f"CoCurve_{tag}_2.txt"), tr)
+            if r is not None:
+                rows[f"{tr:.3f}"] = [r[0], r[1]]
+        out[tag] = rows
+    return out
+
+
+def run_case(name: str, kw: dict, steps: int, src: str):
+    s = O.Setup(**kw)
+    tag = O.TAG_OF_MODEL[s.model]
+    g, l = O.read_cocurve(os.path.join(src, "CoCurve", f"CoCurve_{tag}_2.txt"), s.tr)
+    A, B, Tc, Rc, T = s.constants()
+    st = O.State(s, g * Rc, l * Rc, backend="ref").init()
+    init_dens, init_dist = st.dens.copy(), st.dist.copy()
+    st.step(steps)
+    np.savez_compressed(
+        os.path.join(HERE, f"ref_{name}.npz"),
+        setup=json.dumps({k: v for k, v in kw.items()}),
+        steps=steps, den_g=g * Rc, den_l=l * Rc,
+        type=st.type, init_dens=init_dens, init_dist=init_dist,
+        dens=st.dens, pote=st.pote, dist=st.dist,
+        vx=st.vx, vy=st.vy, vz=st.vz, fx=st.fx, fy=st.fy, fz=st.fz,
+        mvx=st.mvx, mvy=st.mvy, mvz=st.mvz)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--src", default="/root/reference")
+    a = ap.parse_args()
+    if O.build_ref() is None:
+        sys.exit("oracle/_ref could not be built (reference sources unavailable)")
+    with open(os.path.join(HERE, "cocurve_rows.json"), "w") as f:
+        json.dump(cocurve(a.src), f, indent=1, sort_keys=True)
+    for name, (kw, steps) in CASES.items():
+        run_case(name, kw, steps, a.src)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA library (through its C ABI) against the reference's own
+kernels (golden fixtures) and the FP64 oracle.
+
+Tolerances (relative unless stated):
+  PLAIN FP64 vs reference fixture / oracle      1e-11 (different summation
+      order in the factored MRT; CUDA's log/tanh within an ulp of glibc's)
+  PLAIN FP32 vs FP64 oracle, rho                2e-5 after 200 steps
+  FUSED FP32 / FP16 / BF16 vs FP64 oracle, rho  2e-5 / 2e-3 / 1.5e-2 after 100 steps
+  velocities: max |du| / max |u_oracle|         scaled 20x the rho bound
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CASES = sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
+
+
+def load_case(name):
+    z = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    return z, json.loads(str(z["setup"]))
+
+
+def solver_for(cpmp, kw, scheme="plain", storage="f64", den=None, **extra):
+    """Solver with the oracle Setup keyword names translated to cpmp_params."""
+    m = dict(dx=kw["dx"], dy=kw["dy"], dz=kw["dz"])
+    m["model"] = kw.get("model", 202)
+    m["tr"] = kw.get("tr", 0.7)
+    m["k"] = kw.get("K", 0.2)
+    m["ka"] = kw.get("Ka", 0.001)
+    m["k1"] = kw.get("K1", 0.0)
+    m["k2"] = kw.get("K2", 0.0)
+    m["tau"] = kw.get("tau", 0.8)
+    m["base_pt"] = kw.get("base_pt", -0.08)
+    m["wall_mode"] = kw.get("wall_mode", 1)
+    m["lap_order"] = kw.get("lap_order", 5)
+    m["complex_bc"] = kw.get("complex_bc", 1)
+    if "eos_a" in kw:
+        m["eos_a"] = kw["eos_a"]
+    if "eos_b" in kw:
+        m["eos_b"] = kw["eos_b"]
+    if den is not None:
+        m["den_g"], m["den_l"] = den
+    m["scheme"] = cpmp.SCHEME[scheme]
+    m["storage"] = cpmp.STORE[storage]
+    m.update(extra)
+    s = cpmp.Solver(**m)
+    s.set_flow_field(radius=kw.get("radius", 60.0), width=kw.get("width", 10.0),
+                     centre=kw.get("centre"))
+    return s
+
+
+def rel_err(a, b, mask):
+    return float(np.max(np.abs(a[mask] - b[mask]) / np.abs(b[mask])))
+
+
+def vel_err(su, ou, mask):
+    n = mask.size
+    du = max(np.max(np.abs(su[c * n:(c + 1) * n][mask] - ou[c][mask])) for c in range(3))
+    scale = max(np.max(np.abs(ou[c][mask])) for c in range(3))
+    return du / scale
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_plain_fp64_matches_reference_kernels(cpmp, case):
+    z, kw = load_case(case)
+    s = solver_for(cpmp, kw, den=(float(z["den_g"]), float(z["den_l"])))
+    fluid = z["type"] == 1
+    assert np.array_equal(s.get("type"), z["type"])
+    assert rel_err(s.get("rho"), z["init_dens"], fluid) < 1e-15
+    s.step(int(z["steps"]))
+    assert rel_err(s.get("rho"), z["dens"], fluid) < 1e-11
+    u = s.get("u")
+    assert vel_err(u, (z["vx"], z["vy"], z["vz"]), fluid) < 1e-9
+    mv = s.get("mv")
+    assert vel_err(mv, (z["mvx"], z["mvy"], z["mvz"]), fluid) < 1e-9
+    F = s.get("force")
+    assert vel_err(F, (z["fx"], z["fy"], z["fz"]), fluid) < 1e-9
+    mu = s.get("mu")
+    assert float(np.max(np.abs(mu[fluid] - z["pote"][fluid]))) < 1e-12
+    d = s.get("dist").reshape(19, -1)
+    zd = z["dist"].reshape(19, -1)
+    assert float(np.max(np.abs(d[:, fluid] - zd[:, fluid]))) < 1e-12
+    s.close()
+
+
+def oracle_run(O, kw, steps, den):
+    st = O.State(O.Setup(**kw), den[0], den[1], "oracle").init()
+    st.step(steps)
+    return st
+
+
+WALLED = dict(dx=40, dy=16, dz=28, radius=8.0, width=4.0, base_pt=-0.04)
+PERIODIC_CS = dict(dx=32, dy=32, dz=32, radius=8.0, width=2.0, wall_mode=0, centre=(16, 16, 16),
+                   model=206, tr=0.85, eos_a=0.5, eos_b=4.0, Ka=0.01, tau=1.0)
+
+
+@pytest.mark.parametrize("cfg,steps", [(WALLED, 200), (PERIODIC_CS, 200)])
+def test_plain_fp32_vs_fp64_oracle(cpmp, oracle_mod, cfg, steps):
+    co = cpmp.coexistence(cfg.get("model", 202), cfg.get("tr", 0.7), cfg.get("eos_a", 0.0),
+                          cfg.get("eos_b", 0.0))
+    den = (co["den_g"], co["den_l"])
+    st = oracle_run(oracle_mod, cfg, steps, den)
+    s = solver_for(cpmp, cfg, storage="f32", den=den)
+    s.step(steps)
+    fluid = st.type == 1
+    assert rel_err(s.get("rho"), st.dens, fluid) < 2e-5
+    assert vel_err(s.get("u"), (st.vx, st.vy, st.vz), fluid) < 4e-4
+    s.close()
+
+
+@pytest.mark.parametrize("storage,rtol", [("f32", 2e-5), ("f16", 2e-3), ("bf16", 1.5e-2)])
+@pytest.mark.parametrize("cfg", [WALLED, PERIODIC_CS], ids=["walled_prw", "periodic_cs"])
+def test_fused_vs_fp64_oracle(cpmp, oracle_mod, storage, rtol, cfg):
+    steps = 100
+    co = cpmp.coexistence(cfg.get("model", 202), cfg.get("tr", 0.7), cfg.get("eos_a", 0.0),
+                          cfg.get("eos_b", 0.0))
+    den = (co["den_g"], co["den_l"])
+    st = oracle_run(oracle_mod, cfg, steps, den)
+    s = solver_for(cpmp, cfg, scheme="fused", storage=storage, den=den)
+    s.step(steps)
+    fluid = st.type == 1
+    e = rel_err(s.get("rho"), st.dens, fluid)
+    assert e < rtol, e
+    assert vel_err(s.get("u"), (st.vx, st.vy, st.vz), fluid) < 20 * rtol
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,storage", [("plain", "f32"), ("fused", "f32"), ("fused", "f16")])
+def test_set_get_dist_round_trip(cpmp, scheme, storage):
+    cfg = dict(WALLED)
+    s = solver_for(cpmp, cfg, scheme=scheme, storage=storage)
+    s.step(7)
+    d = s.get("dist")
+    s.set("dist", d)
+    d2 = s.get("dist")
+    fluid = s.get("type") == 1
+    a, b = d.reshape(19, -1)[:, fluid], d2.reshape(19, -1)[:, fluid]
+    tol = 0 if storage == "f32" else 2e-3
+    assert float(np.max(np.abs(a - b) / np.maximum(np.abs(a), 1e-3))) <= max(tol, 1e-6)
+    s.close()
+
+
+@pytest.mark.parametrize("scheme,storage", [("plain", "f64"), ("plain", "f32"), ("fused", "f32"),
+                                            ("fused", "f16"), ("fused", "bf16")])
+def test_mass_conservation(cpmp, scheme, storage):
+    s = solver_for(cpmp, WALLED, scheme=scheme, storage=storage)
+    s.step(1)
+    m0 = s.reduce()["mass"]
+    s.step(300)
+    m1 = s.reduce()["mass"]
+    tol = {"f64": 1e-12, "f32": 2e-6, "f16": 2e-4, "bf16": 2e-3}[storage]
+    assert abs(m1 - m0) <= tol * m0, (m0, m1)
+    s.close()
+
+
+def test_step_chunking_is_invisible(cpmp):
+    """Graph replay (2-step chunks) and single launches give the same state."""
+    a = solver_for(cpmp, WALLED, scheme="fused", storage="f16")
+    b = solver_for(cpmp, WALLED, scheme="fused", storage="f16")
+    a.step(9)
+    for _ in range(9):
+        b.step(1)
+    assert np.array_equal(a.get("rho"), b.get("rho"))
+    assert np.array_equal(a.get("dist"), b.get("dist"))
+
+
+def test_contact_angle_on_device_matches_oracle(cpmp, oracle_mod):
+    O = oracle_mod
+    cfg = dict(dx=96, dy=8, dz=40, radius=14.0, width=4.0, base_pt=-0.04)
+    co = cpmp.coexistence(202, 0.7)
+    st = oracle_run(O, cfg, 300, (co["den_g"], co["den_l"]))
+    s = solver_for(cpmp, cfg, storage="f64", den=(co["den_g"], co["den_l"]))
+    s.set("rho", st.dens)
+    d = s.reduce()
+    o = st.contact_angle()
+    for k in ("ca_left", "ca_right", "ca_cap", "x_left", "x_right"):
+        assert d[k] == pytest.approx(o[k], rel=1e-12, abs=1e-12), k
+    m = st.mass()
+    assert d["mass"] == pytest.approx(m[0], rel=1e-13)
+
+
+def test_nonfinite_density_is_reported(cpmp):
+    s = solver_for(cpmp, WALLED, storage="f32")
+    rho = s.get("rho")
+    rho[len(rho) // 2 + 7] = np.nan
+    s.set("rho", rho)
+    with pytest.raises(cpmp.CpmpError) as e:
+        s.reduce()
+    assert e.value.status == 5
+    assert s.reduce(allow_nonfinite=True)["nonfinite"] == 1
