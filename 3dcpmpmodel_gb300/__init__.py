@@ -161,6 +161,16 @@ class Solver:
             _abi.check(rc)
         return {k: getattr(d, k) for k, _ in Diag._fields_}
 
+    def autotune(self) -> dict:
+        """Pick the fused kernel's tile shape and march length by timing them
+        on a scratch copy of the current state."""
+        ty, tz, xl, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _abi.check(self._lib.cpmp_autotune(self._h, C.byref(ty), C.byref(tz), C.byref(xl), C.byref(ms)))
+        return {"tile_y": ty.value, "tile_z": tz.value, "march_x": xl.value, "collide_ms": ms.value}
+
+    def set_tile(self, tile_y: int, tile_z: int, march_x: int):
+        _abi.check(self._lib.cpmp_set_tile(self._h, int(tile_y), int(tile_z), int(march_x)))
+
     # timing ------------------------------------------------------------------------
     @property
     def stream(self) -> int:

@@ -75,6 +75,9 @@ SIGNATURES = {
     "cpmp_get_eos": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_double)] * 6),
     "cpmp_coexistence": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                    C.c_char_p] + [C.POINTER(C.c_double)] * 6),
+    "cpmp_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "cpmp_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "cpmp_stream": (C.c_void_p, [C.c_void_p]),
     "cpmp_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),

@@ -48,6 +48,7 @@ struct cpmp_handle {
     bool f64 = false;  // PLAIN with FP64 storage/arithmetic
     uint8_t *type = nullptr;
     void *rho = nullptr, *mu = nullptr, *u = nullptr, *mv = nullptr, *F = nullptr;
+    void *rho2 = nullptr;  // FUSED: next step's density (swapped with rho every step)
     void *fb[2] = {nullptr, nullptr};
     int cur = 0;
     void *h = nullptr;
@@ -98,12 +99,12 @@ void free_all(cpmp_handle *h)
 {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
-    void *ptrs[] = {h->type, h->rho, h->mu, h->u, h->mv, h->F, h->fb[0], h->fb[1], h->h, h->f0[0], h->f0[1],
+    void *ptrs[] = {h->type, h->rho, h->rho2, h->mu, h->u, h->mv, h->F, h->fb[0], h->fb[1], h->h, h->f0[0], h->f0[1],
                     h->wall, h->partials, h->dout};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     h->type = nullptr;
-    h->rho = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
+    h->rho = h->rho2 = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
     h->f0[0] = h->f0[1] = nullptr;
     h->partials = h->dout = nullptr;
     if (h->st) cudaStreamDestroy(h->st);
@@ -170,10 +171,11 @@ void launch_one_step(cpmp_handle *h, LaunchHook *hook)
     } else {
         auto k = make_kparams<float>(h);
         const int P = (int)(h->step & 1);
-        fused_launch_wall(k, (float *)h->rho, h->st, hook);
+        fused_launch_wall(k, (float *)h->rho, (float *)h->rho2, h->st, hook);
         fused_launch_collide(h->p.storage, k, P, h->tile, h->h, h->f0[P], h->f0[1 - P], (const float *)h->rho,
-                             h->st, hook);
-        fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho, h->st, hook);
+                             (float *)h->rho2, h->st, hook);
+        fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho2, &h->tile, h->st, hook);
+        std::swap(h->rho, h->rho2);
     }
     h->step += 1;
     h->launches += h->launches_per_step;
@@ -417,11 +419,15 @@ cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
         if ((s = dalloc(&h->fb[1], CPMP_Q * n * rs, "f")) != CPMP_OK) return s;
     } else {
         const size_t hs = p.storage == CPMP_STORE_F32 ? 4 : 2;
+        if ((s = dalloc(&h->rho2, n * rs, "rho")) != CPMP_OK) return s;
         if ((s = dalloc(&h->h, (CPMP_Q - 1) * n * hs, "h")) != CPMP_OK) return s;
         if ((s = dalloc((void **)&h->f0[0], n * sizeof(float), "f0")) != CPMP_OK) return s;
         if ((s = dalloc((void **)&h->f0[1], n * sizeof(float), "f0")) != CPMP_OK) return s;
         CK(fused_setup_attributes());
         h->tile = default_tile(p);
+        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz)) h->tile = FusedTile{4, 32, h->tile.xl};
+        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz))
+            return fail(CPMP_ERR_UNSUPPORTED, "no fused tile fits this device's shared memory");
     }
     std::vector<double> w(2 * np, p.base_pt);
     if ((s = upload_wall(h.get(), w)) != CPMP_OK) return s;
@@ -462,6 +468,7 @@ cpmp_status cpmp_init_droplet(cpmp_handle *h, const cpmp_droplet *d)
         CK(cudaMemsetAsync(h->f0[1], 0, n * sizeof(float), h->st));
         fused_launch_init(h->p.storage, make_kparams<float>(h), dd, h->type, (float *)h->rho, h->f0[0], h->h,
                           h->st);
+        CK(cudaMemcpyAsync(h->rho2, h->rho, n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
     }
     h->launches += h->plain ? 1 : 2;
     CK(cudaGetLastError());
@@ -625,7 +632,7 @@ cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *
         auto k = make_kparams<float>(h);
         if (e == cudaSuccess) {
             fused_launch_encode(h->p.storage, k, P, h->h, h->f0[P], tmp, dtype == CPMP_F64, h->st);
-            fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, h->st, nullptr);
+            fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, nullptr, h->st, nullptr);
             h->launches += 3;
             e = cudaStreamSynchronize(h->st);
         }
@@ -698,6 +705,103 @@ cpmp_status cpmp_get_eos(cpmp_handle *h, double *den_g, double *den_l, double *A
     if (B) *B = h->B;
     if (T) *T = h->T;
     if (Rc) *Rc = h->Rc;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, double *ms_per_step)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    CK(cudaSetDevice(h->p.device));
+    if (h->plain) return CPMP_OK;
+    if (!h->initialised) return fail(CPMP_ERR_PARAM, "initialise the state before tuning");
+    const size_t n = (size_t)h->n;
+    const size_t hs = h->p.storage == CPMP_STORE_F32 ? 4 : 2;
+    // scratch copy of the state: the in-place A-A kernel would otherwise advance it
+    void *sh = nullptr, *sf0a = nullptr, *sf0b = nullptr, *srho = nullptr, *srho2 = nullptr;
+    cpmp_status s;
+    if ((s = dalloc(&sh, (CPMP_Q - 1) * n * hs, "tune h")) != CPMP_OK) return s;
+    if ((s = dalloc(&sf0a, n * 4, "tune f0")) != CPMP_OK || (s = dalloc(&sf0b, n * 4, "tune f0")) != CPMP_OK ||
+        (s = dalloc(&srho, n * 4, "tune rho")) != CPMP_OK || (s = dalloc(&srho2, n * 4, "tune rho")) != CPMP_OK) {
+        cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(srho2);
+        return s;
+    }
+    const int P0 = (int)(h->step & 1);
+    cudaMemcpyAsync(sh, h->h, (CPMP_Q - 1) * n * hs, cudaMemcpyDeviceToDevice, h->st);
+    cudaMemcpyAsync(sf0a, h->f0[P0], n * 4, cudaMemcpyDeviceToDevice, h->st);
+    cudaMemcpyAsync(srho, h->rho, n * 4, cudaMemcpyDeviceToDevice, h->st);
+    auto k = make_kparams<float>(h);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    FusedTile best = h->tile;
+    double best_ms = 1e30;
+    const int xls[] = {8, 16, 32, 64, 128};
+    for (int t = 0; t < fused_tile_count(); ++t) {
+        for (int xi = 0; xi < 5; ++xi) {
+            FusedTile ft = fused_tile(t, xls[xi]);
+            if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz)) continue;
+            if (ft.xl > h->p.dx && xi > 0) continue;
+            if (ft.ty > 2 * h->p.dy && ft.ty > 1) continue;
+            if (ft.tz > 2 * h->p.dz) continue;
+            ft.xl = std::min(ft.xl, h->p.dx);
+            // warm-up, then time two launches (one of each parity)
+            fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
+                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+            cudaEventRecord(e0, h->st);
+            fused_launch_collide(h->p.storage, k, 1, ft, sh, (const float *)sf0b, (float *)sf0a,
+                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+            fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
+                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+            cudaEventRecord(e1, h->st);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0); cudaEventDestroy(e1);
+                cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(srho2);
+                return fail(CPMP_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            h->launches += 3;
+            if (ms / 2 < best_ms) {
+                best_ms = ms / 2;
+                best = ft;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sh);
+    cudaFree(sf0a);
+    cudaFree(sf0b);
+    cudaFree(srho);
+    cudaFree(srho2);
+    CK(cudaGetLastError());
+    if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl) {
+        h->tile = best;
+        if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+    }
+    if (tile_y) *tile_y = best.ty;
+    if (tile_z) *tile_z = best.tz;
+    if (march_x) *march_x = best.xl;
+    if (ms_per_step) *ms_per_step = best_ms;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_set_tile(cpmp_handle *h, int tile_y, int tile_z, int march_x)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    if (h->plain) return fail(CPMP_ERR_UNSUPPORTED, "tiles apply to the FUSED scheme");
+    if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
+    if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z))
+        return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
+    h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx)};
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
     return CPMP_OK;
 }
 

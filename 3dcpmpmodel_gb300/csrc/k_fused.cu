@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_velocity(KParams<float> p, int P, const
 
 // ------------------------------------------------------------- dispatch ----
 namespace {
-constexpr int kTiles[][2] = {{4, 32}, {8, 32}, {2, 64}, {1, 128}};
+constexpr int kTiles[][2] = {{4, 32}, {8, 32}, {16, 32}, {2, 64}, {1, 128}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
 template <class F>
@@ -111,38 +111,62 @@ void with_storage(int storage, F &&f)
 
 template <class S, int TY, int TZ, int L>
 void launch_collide_t(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
-                      float *f0n, const float *rho, cudaStream_t st)
+                      float *f0n, const float *rho, float *rho_next, cudaStream_t st)
 {
     const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + t.xl - 1) / t.xl);
-    k_fused_collide<S, TY, TZ, L><<<grid, TY * TZ, fused_smem_bytes<TY, TZ, L>(), st>>>(p, P, h, f0c, f0n, rho, t.xl);
+    k_fused_collide<S, TY, TZ, L><<<grid, TY * TZ, fused_smem_bytes<S, TY, TZ, L>(), st>>>(
+        p, P, h, f0c, f0n, rho, rho_next, t.xl);
 }
 
 template <class S, int L>
 void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
-                      float *f0n, const float *rho, cudaStream_t st)
+                      float *f0n, const float *rho, float *rho_next, cudaStream_t st)
 {
-    if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, st);
-    else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, st);
-    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, st);
-    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, st);
+    if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+    else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+    else if (t.ty == 16 && t.tz == 32) launch_collide_t<S, 16, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+}
+
+// usable[storage index][L - 2][tile index]: the instantiation's shared
+// memory fits the device's opt-in limit
+bool g_usable[3][2][8];
+int storage_index(int storage) { return storage == CPMP_STORE_F16 ? 0 : (storage == CPMP_STORE_BF16 ? 1 : 2); }
+int tile_index(int ty, int tz)
+{
+    for (int i = 0; i < kNumTiles; ++i)
+        if (kTiles[i][0] == ty && kTiles[i][1] == tz) return i;
+    return -1;
 }
 
 template <class S, int TY, int TZ, int L>
-cudaError_t set_attr_t()
+void set_attr_t(int si, int max_smem)
 {
-    return cudaFuncSetAttribute(k_fused_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)fused_smem_bytes<TY, TZ, L>());
+    const size_t b = fused_smem_bytes<S, TY, TZ, L>();
+    bool ok = (int)b <= max_smem;
+    if (ok)
+        ok = cudaFuncSetAttribute(k_fused_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)b) == cudaSuccess;
+    cudaGetLastError();
+    g_usable[si][L - 2][tile_index(TY, TZ)] = ok;
 }
 template <class S, int L>
-cudaError_t set_attr_l()
+void set_attr_l(int si, int max_smem)
 {
-    cudaError_t e;
-    if ((e = set_attr_t<S, 4, 32, L>()) != cudaSuccess) return e;
-    if ((e = set_attr_t<S, 8, 32, L>()) != cudaSuccess) return e;
-    if ((e = set_attr_t<S, 2, 64, L>()) != cudaSuccess) return e;
-    return set_attr_t<S, 1, 128, L>();
+    set_attr_t<S, 4, 32, L>(si, max_smem);
+    set_attr_t<S, 8, 32, L>(si, max_smem);
+    set_attr_t<S, 16, 32, L>(si, max_smem);
+    set_attr_t<S, 2, 64, L>(si, max_smem);
+    set_attr_t<S, 1, 128, L>(si, max_smem);
 }
 }  // namespace
+
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz)
+{
+    const int t = tile_index(ty, tz);
+    return t >= 0 && g_usable[storage_index(storage)][lap_order == 7 ? 1 : 0][t];
+}
 
 int fused_tile_count() { return kNumTiles; }
 FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl}; }
@@ -155,13 +179,17 @@ bool fused_tile_supported(int ty, int tz)
 
 cudaError_t fused_setup_attributes()
 {
-    cudaError_t e;
-    if ((e = set_attr_l<__half, 2>()) != cudaSuccess) return e;
-    if ((e = set_attr_l<__half, 3>()) != cudaSuccess) return e;
-    if ((e = set_attr_l<__nv_bfloat16, 2>()) != cudaSuccess) return e;
-    if ((e = set_attr_l<__nv_bfloat16, 3>()) != cudaSuccess) return e;
-    if ((e = set_attr_l<float, 2>()) != cudaSuccess) return e;
-    return set_attr_l<float, 3>();
+    int dev = 0, max_smem = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+    set_attr_l<__half, 2>(0, max_smem);
+    set_attr_l<__half, 3>(0, max_smem);
+    set_attr_l<__nv_bfloat16, 2>(1, max_smem);
+    set_attr_l<__nv_bfloat16, 3>(1, max_smem);
+    set_attr_l<float, 2>(2, max_smem);
+    set_attr_l<float, 3>(2, max_smem);
+    return cudaSuccess;
 }
 
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
@@ -175,41 +203,43 @@ void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d
     });
 }
 
-void fused_launch_wall(const KParams<float> &p, float *rho, cudaStream_t st, LaunchHook *hook)
+void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, cudaStream_t st, LaunchHook *hook)
 {
     if (p.wall_mode != 1) return;
     const long long np = (long long)p.dx * p.dy;
     const unsigned gw = (unsigned)((np + 127) / 128);
     for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) {
         hook_begin(hook, K_WALL, st);
-        k_wall_pass<float><<<gw, 128, 0, st>>>(p, s, rho, nullptr);
+        k_wall_pass<float><<<gw, 128, 0, st>>>(p, s, rho, nullptr, rho_mirror);
         hook_end(hook, K_WALL, st);
     }
 }
 
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
+                          const float *f0c, float *f0n, const float *rho, float *rho_next, cudaStream_t st,
                           LaunchHook *hook)
 {
     hook_begin(hook, K_FUSED, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
         if (p.lap_order == 7)
-            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, st);
+            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, rho_next, st);
         else
-            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, st);
+            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, rho_next, st);
     });
     hook_end(hook, K_FUSED, st);
 }
 
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
-                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook)
+                          const float *f0, float *rho, const FusedTile *fold, cudaStream_t st, LaunchHook *hook)
 {
-    const unsigned g = (unsigned)((p.n + 255) / 256);
+    const dim3 g((unsigned)((p.dz + 127) / 128), (unsigned)p.dy, (unsigned)p.dx);
+    FoldTile ft{0, 0, 0};
+    if (fold) ft = FoldTile{fold->ty, fold->tz, fold->xl};
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density<S><<<g, 256, 0, st>>>(p, P, (const S *)h, f0, rho);
+        k_density<S><<<g, 128, 0, st>>>(p, P, (const S *)h, f0, rho, ft);
     });
     hook_end(hook, K_DENSITY, st);
 }

@@ -55,6 +55,15 @@ __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >
 __host__ __device__ __forceinline__ constexpr float ratio0(int q) { return q <= 6 ? 1.0f / 6.0f : 1.0f / 12.0f; }
 __host__ __device__ __forceinline__ constexpr float inv_w(int q) { return q <= 6 ? 18.0f : 36.0f; }
 
+// Decoded population: f = w_q h + (w_q / w_0) a, evaluated with explicit
+// rounding (no FMA contraction) so every kernel that decodes the same stored
+// value gets the same float.
+template <class S>
+__device__ __forceinline__ float decode_pop(int q, S hv, float a)
+{
+    return __fadd_rn(__fmul_rn(wgt<float>(q), s2f<S>(hv)), __fmul_rn(ratio0(q), a));
+}
+
 // Post-stream populations of node (i,j,k) at parity P.
 template <class S>
 __device__ __forceinline__ void gather_pops(const KParams<float> &p, int P, const S *__restrict__ h,
@@ -75,7 +84,7 @@ __device__ __forceinline__ void gather_pops(const KParams<float> &p, int P, cons
             hv = s2f<S>(h[(long long)(q - 1) * n + I]);
         else
             hv = s2f<S>(ss ? h[(long long)(q - 1) * n + I] : h[(long long)(opp(q) - 1) * n + src]);
-        f[q] = wgt<float>(q) * hv + ratio0(q) * a;
+        f[q] = __fadd_rn(__fmul_rn(wgt<float>(q), hv), __fmul_rn(ratio0(q), a));
     }
 }
 
@@ -104,180 +113,376 @@ __device__ __forceinline__ void scatter_pops(const KParams<float> &p, int P, S *
 }
 
 // ------------------------------------------------------------ density ----
-// rho = sum of the post-stream populations (MacroCalculate's density,
-// FluidCuda.cu:357-361) on fluid nodes.
-template <class S>
-__global__ void __launch_bounds__(256) k_density(KParams<float> p, int P, const S *__restrict__ h,
-                                                 const float *__restrict__ f0, float *__restrict__ rho)
+// Offset of the neighbour x + e_q in the flat index, for nodes whose
+// neighbours need no periodic wrap.
+__device__ __forceinline__ long long nb_off(int q, int plane, int dz)
 {
-    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= p.n) return;
-    const int k = (int)(I % p.dz);
-    if (solid_k(p.wall_mode, k, p.dz)) return;
-    const int j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    return (long long)cx(q) * plane + (long long)cy(q) * dz + cz(q);
+}
+
+// Is every node of the z-range [z0, z0+tz) and all its +-1 neighbours a fluid
+// node that needs no z wrap?
+__device__ __forceinline__ bool z_interior(const KParams<float> &p, int z0, int tz)
+{
+    return p.wall_mode == 1 ? (z0 >= 4 && z0 + tz <= p.dz - 4) : (z0 >= 1 && z0 + tz <= p.dz - 1);
+}
+
+// Tile-interior node of the fused collide: its post-stream density is
+// computed inside the collide kernel (all 18 sources were collided by the
+// same CTA), so the density pass skips it.
+struct FoldTile {
+    int ty, tz, xl;  // 0 = fold off: the density pass computes every node
+};
+__device__ __forceinline__ bool fold_interior(const KParams<float> &p, const FoldTile &t, int i, int j, int k)
+{
+    if (t.xl <= 0) return false;
+    const int x0 = (i / t.xl) * t.xl, x1 = min(x0 + t.xl, p.dx);
+    const int y0 = (j / t.ty) * t.ty, yn = min(t.ty, p.dy - y0);
+    const int z0 = (k / t.tz) * t.tz, zn = min(t.tz, p.dz - z0);
+    const int ly = j - y0, lz = k - z0;
+    return i >= x0 + 1 && i <= x1 - 2 && ly >= 1 && ly <= yn - 2 && lz >= 1 && lz <= zn - 2;
+}
+
+// rho = sum of the post-stream populations (MacroCalculate's density,
+// FluidCuda.cu:357-361) on fluid nodes: r = f0, then r += f_q for q = 1..18
+// in order, every term decoded by decode_pop.  Grid: (z blocks, dy, dx).
+template <class S>
+__global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const S *__restrict__ h,
+                                                 const float *__restrict__ f0, float *__restrict__ rho,
+                                                 FoldTile fold)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, i = blockIdx.z;
+    if (k >= p.dz || solid_k(p.wall_mode, k, p.dz)) return;
+    if (fold_interior(p, fold, i, j, k)) return;
+    const int plane = p.dy * p.dz;
+    const long long I = ((long long)i * p.dy + j) * p.dz + k;
+    const long long n = p.n;
+    const bool fast = i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy &&
+                      (p.wall_mode == 1 ? (k >= 4 && k <= p.dz - 5) : (k >= 1 && k + 1 < p.dz));
+    if (fast) {
+        float r = f0[I];
+#pragma unroll
+        for (int q = 1; q < Q; ++q) {
+            const long long src = I - nb_off(q, plane, p.dz);
+            const S hv = P == 0 ? h[(long long)(q - 1) * n + I] : h[(long long)(opp(q) - 1) * n + src];
+            r = __fadd_rn(r, decode_pop<S>(q, hv, __ldg(f0 + src)));
+        }
+        rho[I] = r;
+        return;
+    }
     float f[Q];
     gather_pops<S>(p, P, h, f0, i, j, k, I, f);
-    float r = 0.f;
+    float r = f[0];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) r += f[q];
+    for (int q = 1; q < Q; ++q) r = __fadd_rn(r, f[q]);
     rho[I] = r;
 }
 
 // --------------------------------------------------------- fused step ----
 __device__ __forceinline__ int ring_slot(int x, int nr) { return ((x % nr) + nr) % nr; }
-
-// One CTA owns a TY x TZ column tile of (y, z) and marches over XL planes of
-// x.  Rings of shared-memory planes:
-//   rho: planes p-3 .. p+3+L with a (3+L)-deep y/z halo (L = 2 for the
-//        five-point Laplacian, 3 for the seven-point one);
-//   mu : planes p-3 .. p+3 with a 3-deep halo.
-// For output plane p the CTA loads rho(p+3+L), evaluates mu(p+3) (EOS +
-// Laplacian, wall potential on solid nodes), then for every fluid node of
-// plane p: F = -rho grad7(mu) + grad7(rho)/3, gathers the populations,
-// collides (MRT + exact-difference forcing) and streams A-A in place.
-template <class S, int TY, int TZ, int L>
-__global__ void __launch_bounds__(TY *TZ, 1)
-    k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
-                    float *__restrict__ f0n, const float *__restrict__ rho, int xl)
+__device__ __forceinline__ int wrap_small(int a, int n)
 {
-    constexpr int RH = 3 + L;
-    constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
-    constexpr int NR = 7 + L;
-    constexpr int MY = TY + 6, MZ = TZ + 6;
+    while (a < 0) a += n;
+    while (a >= n) a -= n;
+    return a;
+}
+
+template <int TY, int TZ, int L>
+struct FusedGeom {
+    static constexpr int RH = 3 + L;                 // rho halo (y, z)
+    static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
+    static constexpr int NR = 2 * L + 2;             // rho planes x+3-L .. x+4+L (one prefetched)
+    static constexpr int MY = TY + 6, MZ = TZ + 6;   // (rho, mu) pairs, halo 3, planes x-3..x+3
+    static constexpr int AY = TY + 2, AZ = TZ + 2;   // rest populations, halo 1, planes x-1..x+2
+    static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
+    static constexpr int RM_PAIRS = 7 * MY * MZ;
+    static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
+    static constexpr int TAB_INTS = RY + RZ;
+    static constexpr size_t BASE_BYTES = sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
+                                         sizeof(float) * F0_FLOATS + sizeof(int) * TAB_INTS;
+    // post-collision ring: planes x-3 .. x, each 18 stored moving populations
+    // (S) and the new rest population (float) per node
+    template <class S>
+    static constexpr size_t pc_bytes()
+    {
+        return 4 * (size_t)TY * TZ * (18 * sizeof(S) + sizeof(float));
+    }
+    template <class S>
+    static constexpr size_t bytes()
+    {
+        return ((BASE_BYTES + 15) / 16) * 16 + pc_bytes<S>();
+    }
+};
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ int mod_small(int t, int m)
+{
+    return t < 0 ? t + m : (t >= m ? t - m : t);
+}
+
+// One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
+// x.  Shared-memory rings:
+//   rho : planes x+3-L .. x+4+L, halo 3+L (L = 2: five-point Laplacian, 3: seven-point)
+//   (rho, mu) pairs: planes x-3 .. x+3, halo 3 (the force stencil's support)
+//   f0  : planes x-1 .. x+2, halo 1 (anchors of the moving populations)
+// The next plane's rho and f0 are copied in with cp.async while the current
+// plane is computed, and the next plane's moving populations are loaded into
+// registers, so global-memory latency overlaps the stencil and collision work.
+// For output plane x: mu(x+3) is evaluated (EOS + Laplacian; wall potential on
+// solid nodes), then every fluid node of plane x computes
+// F = -rho grad7(mu) + grad7(rho)/3, decodes its populations, collides (MRT +
+// exact-difference forcing) and streams A-A in place.
+template <class S, int TY, int TZ, int L>
+__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
+    k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
+                    float *__restrict__ f0n, const float *__restrict__ rho, float *__restrict__ rho_next,
+                    int xl)
+{
+    using G = FusedGeom<TY, TZ, L>;
+    constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
+    constexpr int AY = G::AY, AZ = G::AZ;
     constexpr int NT = TY * TZ;
-    extern __shared__ float sm[];
-    float *srho = sm;
-    float *smu = sm + NR * RY * RZ;
+    extern __shared__ float4 smem4[];
+    float *srho = reinterpret_cast<float *>(smem4);
+    float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
+    float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
+    int *tabY = reinterpret_cast<int *>(sf0 + G::F0_FLOATS);
+    int *tabZ = tabY + RY;
+    unsigned char *pc_base = reinterpret_cast<unsigned char *>(smem4) + ((G::BASE_BYTES + 15) / 16) * 16;
+    constexpr int NTILE = TY * TZ;
+    // ring slot r: S h[18][NTILE] followed by float f0[NTILE]
+    auto pc_h = [&](int slot) { return reinterpret_cast<S *>(pc_base + (size_t)slot * NTILE * (18 * sizeof(S) + 4)); };
+    auto pc_f0 = [&](int slot) { return reinterpret_cast<float *>(pc_h(slot) + 18 * NTILE); };
 
     const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
     const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY;
     const int x0 = blockIdx.z * xl;
     const int x1 = min(x0 + xl, p.dx);
+    const int plane = p.dy * p.dz;
+    const long long n = p.n;
+    const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
+    const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
 
-    auto load_rho = [&](int xlog) {
-        const int gx = wrapm(xlog, p.dx);
+    // wrapped y / z coordinates of the halo rows and columns
+    for (int e = threadIdx.x; e < RY + RZ; e += NT) {
+        if (e < RY) tabY[e] = wrap_small(y0 - RH + e, p.dy);
+        else tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+    }
+    __syncthreads();
+
+    auto issue_rho = [&](int xlog) {
+        const long long base = (long long)wrapm(xlog, p.dx) * p.dy;
         float *dst = srho + ring_slot(xlog, NR) * (RY * RZ);
-        const long long base = (long long)gx * p.dy;
         for (int e = threadIdx.x; e < RY * RZ; e += NT) {
             const int ly = e / RZ, lz = e - ly * RZ;
-            const int gy = wrapm(y0 - RH + ly, p.dy), gz = wrapm(z0 - RH + lz, p.dz);
-            dst[e] = __ldg(rho + (base + gy) * p.dz + gz);
+            cp_async4(dst + e, rho + (base + tabY[ly]) * p.dz + tabZ[lz]);
+        }
+    };
+    auto issue_f0 = [&](int xlog) {
+        const long long base = (long long)wrapm(xlog, p.dx) * p.dy;
+        float *dst = sf0 + ring_slot(xlog, 4) * (AY * AZ);
+        for (int e = threadIdx.x; e < AY * AZ; e += NT) {
+            const int ly = e / AZ, lz = e - ly * AZ;
+            cp_async4(dst + e, f0c + (base + tabY[ly + RH - 1]) * p.dz + tabZ[lz + RH - 1]);
         }
     };
     auto comp_mu = [&](int xlog) {
         const int gx = wrapm(xlog, p.dx);
-        float *dst = smu + ring_slot(xlog, 7) * (MY * MZ);
+        float2 *dst = srm + ring_slot(xlog, 7) * (MY * MZ);
         const float *rc = srho + ring_slot(xlog, NR) * (RY * RZ);
         const float *rm1 = srho + ring_slot(xlog - 1, NR) * (RY * RZ);
         const float *rp1 = srho + ring_slot(xlog + 1, NR) * (RY * RZ);
         const float *rm2 = srho + ring_slot(xlog - 2, NR) * (RY * RZ);
         const float *rp2 = srho + ring_slot(xlog + 2, NR) * (RY * RZ);
+        const float *rm3 = L == 3 ? srho + ring_slot(xlog - 3, NR) * (RY * RZ) : rc;
+        const float *rp3 = L == 3 ? srho + ring_slot(xlog + 3, NR) * (RY * RZ) : rc;
         for (int e = threadIdx.x; e < MY * MZ; e += NT) {
             const int my = e / MZ, mz = e - my * MZ;
-            const int gz = wrapm(z0 - 3 + mz, p.dz);
-            if (solid_k(p.wall_mode, gz, p.dz)) {
-                const int gy = wrapm(y0 - 3 + my, p.dy);
-                dst[e] = p.wall[(gz < 3 ? 0 : (long long)p.dx * p.dy) + (long long)gx * p.dy + gy];
-                continue;
-            }
             const int c = (my + L) * RZ + (mz + L);
             const float r0 = rc[c];
+            const int gz = tabZ[mz + L];
+            if (solid_k(p.wall_mode, gz, p.dz)) {
+                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : (long long)p.dx * p.dy) + (long long)gx * p.dy + tabY[my + L]]);
+                continue;
+            }
             float lap;
             if (L == 2) {
                 lap = (-r0 * 90.f + (-rm2[c] + rm1[c] * 16.f + rp1[c] * 16.f - rp2[c]) +
                        (-rc[c - 2 * RZ] + rc[c - RZ] * 16.f + rc[c + RZ] * 16.f - rc[c + 2 * RZ]) +
-                       (-rc[c - 2] + rc[c - 1] * 16.f + rc[c + 1] * 16.f - rc[c + 2])) /
-                      12.f;
+                       (-rc[c - 2] + rc[c - 1] * 16.f + rc[c + 1] * 16.f - rc[c + 2])) *
+                      (1.f / 12.f);
             } else {
-                const float *rm3 = srho + ring_slot(xlog - 3, NR) * (RY * RZ);
-                const float *rp3 = srho + ring_slot(xlog + 3, NR) * (RY * RZ);
                 lap = (-r0 * 1470.f +
                        (2.f * rm3[c] - 27.f * rm2[c] + 270.f * rm1[c] + 270.f * rp1[c] - 27.f * rp2[c] + 2.f * rp3[c]) +
                        (2.f * rc[c - 3 * RZ] - 27.f * rc[c - 2 * RZ] + 270.f * rc[c - RZ] + 270.f * rc[c + RZ] -
                         27.f * rc[c + 2 * RZ] + 2.f * rc[c + 3 * RZ]) +
                        (2.f * rc[c - 3] - 27.f * rc[c - 2] + 270.f * rc[c - 1] + 270.f * rc[c + 1] -
-                        27.f * rc[c + 2] + 2.f * rc[c + 3])) /
-                      180.f;
+                        27.f * rc[c + 2] + 2.f * rc[c + 3])) *
+                      (1.f / 180.f);
             }
-            dst[e] = p.kk * mu0<float>(p.eos, p.A, p.B, p.T, r0) - p.ka * lap;
+            dst[e] = make_float2(r0, p.kk * mu0_fast(eos, r0) - p.ka * lap);
         }
     };
 
-    // prologue: mu(x0-3 .. x0+2)
-    for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) load_rho(x);
-    __syncthreads();
-    comp_mu(x0 - 3);
-    __syncthreads();
-    for (int x = x0 - 2; x <= x0 + 2; ++x) {
-        load_rho(x + L);
-        __syncthreads();
-        comp_mu(x);
-        __syncthreads();
-    }
-
     const int gy = y0 + ty, gz = z0 + tz;
     const bool active = gy < p.dy && gz < p.dz && !solid_k(p.wall_mode, gz, p.dz);
-    for (int x = x0; x < x1; ++x) {
-        load_rho(x + 3 + L);
+
+    // moving populations of one node of plane x into registers (A-A read slots)
+    auto fetch = [&](int x, S hv[Q - 1]) {
+        if (!active) return;
+        const int gx = wrapm(x, p.dx);
+        const long long I = ((long long)gx * p.dy + gy) * p.dz + gz;
+        if (P == 0) {
+#pragma unroll
+            for (int q = 1; q < Q; ++q) hv[q - 1] = h[(long long)(q - 1) * n + I];
+        } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
+#pragma unroll
+            for (int q = 1; q < Q; ++q) hv[q - 1] = h[(long long)(opp(q) - 1) * n + I - nb_off(q, plane, p.dz)];
+        } else {
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const int si = wrap1(gx - cx(q), p.dx), sj = wrap1(gy - cy(q), p.dy), sk = wrap1(gz - cz(q), p.dz);
+                if (solid_k(p.wall_mode, sk, p.dz))
+                    hv[q - 1] = h[(long long)(q - 1) * n + I];
+                else
+                    hv[q - 1] = h[(long long)(opp(q) - 1) * n + ((long long)si * p.dy + sj) * p.dz + sk];
+            }
+        }
+    };
+
+    // Post-stream density of the tile-interior nodes of plane xf, from the
+    // post-collision ring (planes xf-1 .. xf+1): the same decode and the same
+    // summation order as k_density, so the result is bit-identical.
+    const int yn = min(TY, p.dy - y0), zn = min(TZ, p.dz - z0);
+    auto fold_density = [&](int xf) {
+        if (!(active && ty >= 1 && ty <= yn - 2 && tz >= 1 && tz <= zn - 2)) return;
+        const int sb[3] = {ring_slot(xf - 1, 4), ring_slot(xf, 4), ring_slot(xf + 1, 4)};
+        const int me = threadIdx.x;
+        float r = pc_f0(sb[1])[me];
+#pragma unroll
+        for (int q = 1; q < Q; ++q) {
+            const int sk = gz - cz(q);
+            const bool ss = p.wall_mode == 1 && (sk < 3 || sk > p.dz - 4);
+            float v;
+            if (ss) {
+                v = decode_pop<S>(q, pc_h(sb[1])[(opp(q) - 1) * NTILE + me], pc_f0(sb[1])[me]);
+            } else {
+                const int src = me - cy(q) * TZ - cz(q);
+                const int slot = sb[1 - cx(q)];
+                v = decode_pop<S>(q, pc_h(slot)[(q - 1) * NTILE + src], pc_f0(slot)[src]);
+            }
+            r = __fadd_rn(r, v);
+        }
+        rho_next[((long long)wrapm(xf, p.dx) * p.dy + gy) * p.dz + gz] = r;
+    };
+
+    // prologue: mu(x0-3 .. x0+2); f0(x0-1 .. x0+1) and rho(x0+3+L) in flight
+    S hv[Q - 1];
+    for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) issue_rho(x);
+    issue_f0(x0 - 1);
+    issue_f0(x0);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    comp_mu(x0 - 3);
+    for (int x = x0 - 2; x <= x0 + 2; ++x) {
         __syncthreads();
+        issue_rho(x + L);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        comp_mu(x);
+    }
+    __syncthreads();
+    issue_rho(x0 + 3 + L);
+    issue_f0(x0 + 1);
+    cp_async_commit();
+    fetch(x0, hv);
+
+    const int mc = (ty + 3) * MZ + (tz + 3);
+    const int ac = (ty + 1) * AZ + (tz + 1);
+    for (int x = x0; x < x1; ++x) {
+        cp_async_wait_all();
+        __syncthreads();  // rho(x+3+L), f0(x+1) landed; plane x-1 fully done
+        if (x + 1 < x1) {
+            issue_rho(x + 4 + L);
+            issue_f0(x + 2);
+        }
+        cp_async_commit();
+        S hn[Q - 1];
+        if (x + 1 < x1) fetch(x + 1, hn);
+        if (x - 2 >= x0 + 1) fold_density(x - 2);
         comp_mu(x + 3);
         __syncthreads();
         if (active) {
-            // gradients from the rings
-            float gm[3] = {0.f, 0.f, 0.f}, gr[3] = {0.f, 0.f, 0.f};
-            const float *mpl[7], *rpl[7];
+            // force from the (rho, mu) ring
+            const int s7 = ring_slot(x, 7);
+            const float2 *pl[7];
 #pragma unroll
-            for (int d = -3; d <= 3; ++d) {
-                mpl[d + 3] = smu + ring_slot(x + d, 7) * (MY * MZ);
-                rpl[d + 3] = srho + ring_slot(x + d, NR) * (RY * RZ);
-            }
-            const int mc = (ty + 3) * MZ + (tz + 3);
-            const int rcn = (ty + RH) * RZ + (tz + RH);
-            // first difference along line s at distance d: c_d (v(+d) - v(-d))
-            auto line = [&](int sx, int sy, int sz, float &om, float &orr) {
-                float am = 0.f, ar = 0.f;
+            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + mod_small(s7 + d, 7) * (MY * MZ);
+            // (rho, mu) pairs: each first difference is one paired add and one
+            // paired fma per stencil distance (Blackwell FADD2 / FFMA2)
+            float2 g0 = make_float2(0.f, 0.f), g1 = g0, g2 = g0;  // (grad rho, grad mu) per axis
+            auto line = [&](int sx, int sy, int sz) -> float2 {
+                float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int d = 1; d <= 3; ++d) {
                     const float c = d == 1 ? 45.f : (d == 2 ? -9.f : 1.f);
-                    const int mo = sy * d * MZ + sz * d, ro = sy * d * RZ + sz * d;
-                    am += c * (mpl[3 + sx * d][mc + mo] - mpl[3 - sx * d][mc - mo]);
-                    ar += c * (rpl[3 + sx * d][rcn + ro] - rpl[3 - sx * d][rcn - ro]);
+                    const int mo = sy * d * MZ + sz * d;
+                    const float2 a = pl[3 + sx * d][mc + mo], b = pl[3 - sx * d][mc - mo];
+                    acc = __ffma2_rn(make_float2(c, c), __fadd2_rn(a, make_float2(-b.x, -b.y)), acc);
                 }
-                om = am;
-                orr = ar;
+                return acc;
             };
-            float lm, lr;
-            line(1, 0, 0, lm, lr); gm[0] += 2.f * lm; gr[0] += 2.f * lr;
-            line(0, 1, 0, lm, lr); gm[1] += 2.f * lm; gr[1] += 2.f * lr;
-            line(0, 0, 1, lm, lr); gm[2] += 2.f * lm; gr[2] += 2.f * lr;
-            line(1, 1, 0, lm, lr); gm[0] += lm; gm[1] += lm; gr[0] += lr; gr[1] += lr;
-            line(1, -1, 0, lm, lr); gm[0] += lm; gm[1] -= lm; gr[0] += lr; gr[1] -= lr;
-            line(1, 0, 1, lm, lr); gm[0] += lm; gm[2] += lm; gr[0] += lr; gr[2] += lr;
-            line(1, 0, -1, lm, lr); gm[0] += lm; gm[2] -= lm; gr[0] += lr; gr[2] -= lr;
-            line(0, 1, 1, lm, lr); gm[1] += lm; gm[2] += lm; gr[1] += lr; gr[2] += lr;
-            line(0, 1, -1, lm, lr); gm[1] += lm; gm[2] -= lm; gr[1] += lr; gr[2] -= lr;
+            const float2 two = make_float2(2.f, 2.f);
+            float2 l;
+            l = line(1, 0, 0); g0 = __ffma2_rn(two, l, g0);
+            l = line(0, 1, 0); g1 = __ffma2_rn(two, l, g1);
+            l = line(0, 0, 1); g2 = __ffma2_rn(two, l, g2);
+            l = line(1, 1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, l);
+            l = line(1, -1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, make_float2(-l.x, -l.y));
+            l = line(1, 0, 1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, l);
+            l = line(1, 0, -1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
+            l = line(0, 1, 1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, l);
+            l = line(0, 1, -1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
             const float inv360 = 1.0f / 360.0f;
-            const float r = rpl[3][rcn];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                gm[a] *= inv360;
-                gr[a] *= inv360;
-            }
+            const float gm[3] = {g0.y * inv360, g1.y * inv360, g2.y * inv360};
+            const float gr[3] = {g0.x * inv360, g1.x * inv360, g2.x * inv360};
+            const float r = pl[3][mc].x;
             const float Fx = -gm[0] * r + gr[0] * (1.0f / 3.0f);
             const float Fy = -gm[1] * r + gr[1] * (1.0f / 3.0f);
             const float Fz = -gm[2] * r + gr[2] * (1.0f / 3.0f);
 
-            const int gxw = wrapm(x, p.dx);
-            const long long I = ((long long)gxw * p.dy + gy) * p.dz + gz;
+            // decode with the sources' rest populations as anchors
+            const int s4 = ring_slot(x, 4);
+            const float *fa[3];
+            fa[0] = sf0 + mod_small(s4 - 1, 4) * (AY * AZ);  // plane x-1
+            fa[1] = sf0 + s4 * (AY * AZ);                    // plane x
+            fa[2] = sf0 + mod_small(s4 + 1, 4) * (AY * AZ);  // plane x+1
+            const float a0 = fa[1][ac];
             float f[Q];
-            gather_pops<S>(p, P, h, f0c, gxw, gy, gz, I, f);
+            f[0] = a0;
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const int sk = gz - cz(q);
+                const bool ss = !yz_fast && p.wall_mode == 1 && (sk < 3 || sk > p.dz - 4);
+                const float a = ss ? a0 : fa[1 - cx(q)][ac - cy(q) * AZ - cz(q)];
+                f[q] = wgt<float>(q) * s2f<S>(hv[q - 1]) + ratio0(q) * a;
+            }
             const float ir = 1.0f / r;
             const float ux = (f[1] + f[7] + f[9] + f[11] + f[13] - f[2] - f[8] - f[10] - f[12] - f[14]) * ir;
             const float uy = (f[3] + f[7] + f[8] + f[15] + f[17] - f[4] - f[9] - f[10] - f[16] - f[18]) * ir;
             const float uz = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) * ir;
-            float qp[Q];
-            const float *qpp = nullptr;
             if (p.qp) {
+                float qp[Q];
 #pragma unroll
                 for (int a = 0; a < Q; ++a) qp[a] = 0.f;
                 qp[1] = -19.f * (p.k1 + 3.f * p.k2) * (gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
@@ -286,19 +491,56 @@ __global__ void __launch_bounds__(TY *TZ, 1)
                 qp[13] = -p.k1 * gr[0] * gr[1];
                 qp[14] = -p.k1 * gr[2] * gr[1];
                 qp[15] = -p.k1 * gr[0] * gr[2];
-                qpp = qp;
+                collide_mrt_edm<float>(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, qp);
+            } else {
+                collide_mrt_edm<float>(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, nullptr);
             }
-            collide_mrt_edm<float>(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, qpp);
-            scatter_pops<S>(p, P, h, f0n, gxw, gy, gz, I, f);
+
+            // encode against this node's new rest population and stream
+            const int gx = wrapm(x, p.dx);
+            const long long I = ((long long)gx * p.dy + gy) * p.dz + gz;
+            const float an = f[0];
+            f0n[I] = an;
+            // keep the stored values for the in-tile density of this plane
+            {
+                const int sl = ring_slot(x, 4);
+                S *ph = pc_h(sl);
+                pc_f0(sl)[threadIdx.x] = an;
+#pragma unroll
+                for (int q = 1; q < Q; ++q) ph[(q - 1) * NTILE + threadIdx.x] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+            }
+            if (P == 0) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q)
+                    h[(long long)(opp(q) - 1) * n + I] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+            } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q)
+                    h[(long long)(q - 1) * n + I + nb_off(q, plane, p.dz)] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+            } else {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const S v = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                    const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy), dk = wrap1(gz + cz(q), p.dz);
+                    if (solid_k(p.wall_mode, dk, p.dz))
+                        h[(long long)(opp(q) - 1) * n + I] = v;
+                    else
+                        h[(long long)(q - 1) * n + ((long long)di * p.dy + dj) * p.dz + dk] = v;
+                }
+            }
         }
-        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < Q - 1; ++q) hv[q] = hn[q];
     }
+    __syncthreads();
+    if (x1 - 2 >= x0 + 1) fold_density(x1 - 2);
+    cp_async_wait_all();
 }
 
-template <int TY, int TZ, int L>
+template <class S, int TY, int TZ, int L>
 constexpr size_t fused_smem_bytes()
 {
-    return sizeof(float) * ((size_t)(7 + L) * (TY + 2 * (3 + L)) * (TZ + 2 * (3 + L)) + (size_t)7 * (TY + 6) * (TZ + 6));
+    return FusedGeom<TY, TZ, L>::template bytes<S>();
 }
 
 // ------------------------------------------------------------ init etc ----

@@ -17,6 +17,19 @@ __device__ __forceinline__ int wrap_off(int a, int n)
     return a;
 }
 
+// Node of a 3-D launch: grid (z blocks, DY, DX), threads along z.
+#define NODE3D(p)                                                        \
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;                 \
+    const int j = blockIdx.y, i = blockIdx.z;                            \
+    if (k >= (p).dz) return;                                             \
+    const long long I = ((long long)i * (p).dy + j) * (p).dz + k
+
+template <class R>
+__host__ __forceinline__ dim3 grid3(const KParams<R> &p, int bs)
+{
+    return dim3((unsigned)((p.dz + bs - 1) / bs), (unsigned)p.dy, (unsigned)p.dx);
+}
+
 template <class R>
 __device__ __forceinline__ long long nid(const KParams<R> &p, int i, int j, int k)
 {
@@ -70,7 +83,7 @@ __device__ __forceinline__ R wall_extrap(const KParams<R> &p, const R *rho, int 
 }
 
 template <class R>
-__global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu)
+__global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu, R *mirror = nullptr)
 {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (long long)p.dx * p.dy) return;
@@ -80,6 +93,10 @@ __global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu)
         const R b = wall_extrap(p, rho, i, j, 3), t = wall_extrap(p, rho, i, j, D - 4);
         rho[nid(p, i, j, 0)] = rho[nid(p, i, j, 1)] = rho[nid(p, i, j, 2)] = b;
         rho[nid(p, i, j, D - 3)] = rho[nid(p, i, j, D - 2)] = rho[nid(p, i, j, D - 1)] = t;
+        if (mirror) {
+            mirror[nid(p, i, j, 0)] = mirror[nid(p, i, j, 1)] = mirror[nid(p, i, j, 2)] = b;
+            mirror[nid(p, i, j, D - 3)] = mirror[nid(p, i, j, D - 2)] = mirror[nid(p, i, j, D - 1)] = t;
+        }
         if (mu) {
             const R wb = p.wall[c], wt = p.wall[(long long)p.dx * p.dy + c];
             mu[nid(p, i, j, 0)] = mu[nid(p, i, j, 1)] = mu[nid(p, i, j, 2)] = wb;
@@ -89,10 +106,18 @@ __global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu)
         const R b = wall_extrap(p, rho, i, j, 2), t = wall_extrap(p, rho, i, j, D - 3);
         rho[nid(p, i, j, 1)] = b;
         rho[nid(p, i, j, D - 2)] = t;
+        if (mirror) {
+            mirror[nid(p, i, j, 1)] = b;
+            mirror[nid(p, i, j, D - 2)] = t;
+        }
     } else {
         const R b = wall_extrap(p, rho, i, j, 1), t = wall_extrap(p, rho, i, j, D - 2);
         rho[nid(p, i, j, 0)] = b;
         rho[nid(p, i, j, D - 1)] = t;
+        if (mirror) {
+            mirror[nid(p, i, j, 0)] = b;
+            mirror[nid(p, i, j, D - 1)] = t;
+        }
     }
 }
 
@@ -167,9 +192,8 @@ __device__ __forceinline__ void grad7_g(const KParams<R> &p, const R *x, int i, 
 template <class R>
 __global__ void k_chem_potential(KParams<R> p, const uint8_t *type, const R *rho, R *mu)
 {
-    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= p.n || type[I] != FLUID) return;
-    const int k = (int)(I % p.dz), j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    NODE3D(p);
+    if (type[I] != FLUID) return;
     const R m0 = mu0<R>(p.eos, p.A, p.B, p.T, rho[I]);
     if (p.lap_order == 7)
         mu[I] = p.kk * m0 - p.ka * lap7sum_g(p, rho, i, j, k) / R(180);
@@ -181,9 +205,8 @@ __global__ void k_chem_potential(KParams<R> p, const uint8_t *type, const R *rho
 template <class R>
 __global__ void k_force(KParams<R> p, const uint8_t *type, const R *rho, const R *mu, R *F)
 {
-    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= p.n || type[I] != FLUID) return;
-    const int k = (int)(I % p.dz), j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    NODE3D(p);
+    if (type[I] != FLUID) return;
     R gm[3], gr[3];
     grad7_g(p, mu, i, j, k, gm);
     grad7_g(p, rho, i, j, k, gr);
@@ -201,9 +224,8 @@ __global__ void __launch_bounds__(128) k_collide_plain(KParams<R> p, const uint8
                                                        const R *rho, const R *u, const R *F,
                                                        const S *fc, S *fn, R *mv)
 {
-    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= p.n || type[I] != FLUID) return;
-    const int k = (int)(I % p.dz), j = (int)((I / p.dz) % p.dy), i = (int)(I / p.dz / p.dy);
+    NODE3D(p);
+    if (type[I] != FLUID) return;
     const long long n = p.n;
     const R r = rho[I], ux = u[I], uy = u[I + n], uz = u[I + 2 * n];
     const R Fx = F[I], Fy = F[I + n], Fz = F[I + 2 * n];
@@ -245,8 +267,8 @@ __global__ void __launch_bounds__(128) k_collide_plain(KParams<R> p, const uint8
 template <class R, class S>
 __global__ void k_macro(KParams<R> p, const uint8_t *type, const S *f, R *rho, R *u)
 {
-    const long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= p.n || type[I] != FLUID) return;
+    NODE3D(p);
+    if (type[I] != FLUID) return;
     const long long n = p.n;
     R v[Q];
 #pragma unroll
@@ -273,7 +295,7 @@ template <class R, class S>
 void plain_launch_step(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *u, R *F, R *mv,
                        const S *fc, S *fn, cudaStream_t st, LaunchHook *hook)
 {
-    const unsigned g = (unsigned)((p.n + 127) / 128);
+    const dim3 g = grid3(p, 128);
     if (p.wall_mode == 1) {
         const long long np = (long long)p.dx * p.dy;
         const unsigned gw = (unsigned)((np + 127) / 128);
@@ -302,7 +324,7 @@ template <class R, class S>
 void plain_launch_macro(const KParams<R> &p, const uint8_t *type, const S *f, R *rho, R *u,
                         cudaStream_t st)
 {
-    const unsigned g = (unsigned)((p.n + 127) / 128);
+    const dim3 g = grid3(p, 128);
     k_macro<R, S><<<g, 128, 0, st>>>(p, type, f, rho, u);
 }
 
@@ -311,7 +333,7 @@ template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
                            cudaStream_t st)
 {
-    const unsigned g = (unsigned)((p.n + 127) / 128);
+    const dim3 g = grid3(p, 128);
     if (p.wall_mode == 1) {
         const long long np = (long long)p.dx * p.dy;
         const unsigned gw = (unsigned)((np + 127) / 128);

@@ -42,16 +42,24 @@ struct FusedTile {
 int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
 bool fused_tile_supported(int ty, int tz);
+// The (storage, Laplacian, tile) instantiation fits this device's shared memory.
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz);
 
 cudaError_t fused_setup_attributes();
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
                        float *rho, float *f0, void *h, cudaStream_t st);
-void fused_launch_wall(const KParams<float> &p, float *rho, cudaStream_t st, LaunchHook *hook);
+// Wall extrapolation on rho; every value written is mirrored into
+// rho_mirror when it is non-null (the other density buffer).
+void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, cudaStream_t st, LaunchHook *hook);
+// The fused collide reads rho (this step's density) and writes the next
+// step's density of its tile-interior nodes into rho_next.
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
+                          const float *f0c, float *f0n, const float *rho, float *rho_next, cudaStream_t st,
                           LaunchHook *hook);
+// Density of the post-stream populations at parity P.  With fold != null,
+// the nodes the fused collide with that tile already wrote are skipped.
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
-                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook);
+                          const float *f0, float *rho, const FusedTile *fold, cudaStream_t st, LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).
 void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,

@@ -101,6 +101,42 @@ __device__ __forceinline__ R mu0(int eos, R A, R B, R T, R rho)
            T / (R(1) - bd) - A * d / (R(1) + bd * R(2) - bd * bd);
 }
 
+// Single-precision mu0 for the fused kernel: the same expressions with the
+// per-launch constants hoisted, one reciprocal per distinct denominator and
+// the hardware log2 (__logf: absolute error 2^-21.4 near 1, 3 ulp elsewhere;
+// mu is a sum of O(0.1) terms, so this stays at FP32 rounding level).
+#ifdef __CUDACC__
+struct EosFast {
+    int eos;
+    float A, B, T, c_att;  // c_att: A/(2 sqrt2 B) (PR) or A/B (RK)
+};
+__device__ __forceinline__ EosFast make_eos_fast(int eos, float A, float B, float T)
+{
+    EosFast e{eos, A, B, T, 0.f};
+    if (eos == 0) e.c_att = A / (1.41421356237f * 2.0f * B);
+    if (eos == 3) e.c_att = A / B;
+    return e;
+}
+__device__ __forceinline__ float mu0_fast(const EosFast &e, float rho)
+{
+    const float R0 = 9.7f, W0 = 1.5f;
+    float d = rho;
+    if (d > R0) d = R0 + __fdividef(d - R0, 1.0f + (d - R0) * W0);
+    const float bd = e.B * d;
+    const float ir = __frcp_rn(1.0f - bd);
+    if (e.eos == 2) {
+        const float om3 = ir * ir * ir;
+        return e.T * __logf(d) + e.T + e.T * (8.f * bd - 9.f * bd * bd + 3.f * bd * bd * bd) * om3 - 2.f * e.A * d;
+    }
+    const float base = e.T * __logf(d * ir) + e.T * ir;
+    if (e.eos == 1) return base - 2.f * e.A * d;
+    if (e.eos == 3) return base - e.c_att * __logf(1.0f + bd) - e.A * d * __frcp_rn(1.0f + bd);
+    const float s2 = 1.41421356237f;
+    return base - e.c_att * __logf((s2 - 1.0f + bd) * __frcp_rn(s2 + 1.0f - bd)) -
+           e.A * d * __frcp_rn(1.0f + bd * 2.0f - bd * bd);
+}
+#endif  // __CUDACC__
+
 // ---------------------------------------------------------------------------
 // MRT collision + exact-difference forcing, in moment space.
 //
@@ -121,17 +157,17 @@ __device__ __forceinline__ void meq_moments(R rho, R ux, R uy, R uz, R me[Q])
     me[1] = rho * (R(-11) + R(19) * u2);
     me[2] = rho * (R(3) - R(5.5) * u2);
     me[3] = rho * ux;
-    me[4] = rho * ux * R(-2) / R(3);
+    me[4] = rho * ux * R(-2.0 / 3.0);
     me[5] = rho * uy;
-    me[6] = rho * uy * R(-2) / R(3);
+    me[6] = rho * uy * R(-2.0 / 3.0);
     me[7] = rho * uz;
-    me[8] = rho * uz * R(-2) / R(3);
+    me[8] = rho * uz * R(-2.0 / 3.0);
     const R pxx = rho * (ux * ux * R(2) - uy * uy - uz * uz);
     const R pww = rho * (uy * uy - uz * uz);
     me[9] = pxx;
-    me[10] = pxx / R(-2);
+    me[10] = pxx * R(-0.5);
     me[11] = pww;
-    me[12] = pww / R(-2);
+    me[12] = pww * R(-0.5);
     me[13] = rho * ux * uy;
     me[14] = rho * uy * uz;
     me[15] = rho * ux * uz;
@@ -184,12 +220,14 @@ __device__ __forceinline__ void moments(const R f[Q], R m[Q])
 template <class R>
 __device__ __forceinline__ void inverse_moments(const R m[Q], R f[Q])
 {
-    const R n0 = m[0] / R(19), n1 = m[1] / R(2394), n2 = m[2] / R(252);
-    const R n3 = m[3] / R(10), n4 = m[4] / R(40), n5 = m[5] / R(10), n6 = m[6] / R(40);
-    const R n7 = m[7] / R(10), n8 = m[8] / R(40);
-    const R n9 = m[9] / R(36), n10 = m[10] / R(72), n11 = m[11] / R(12), n12 = m[12] / R(24);
-    const R n13 = m[13] / R(4), n14 = m[14] / R(4), n15 = m[15] / R(4);
-    const R n16 = m[16] / R(8), n17 = m[17] / R(8), n18 = m[18] / R(8);
+    // multiply by the rounded reciprocals of the row norms (no divisions)
+    const R n0 = m[0] * (R(1) / R(19)), n1 = m[1] * (R(1) / R(2394)), n2 = m[2] * (R(1) / R(252));
+    const R n3 = m[3] * R(0.1), n4 = m[4] * R(0.025), n5 = m[5] * R(0.1), n6 = m[6] * R(0.025);
+    const R n7 = m[7] * R(0.1), n8 = m[8] * R(0.025);
+    const R n9 = m[9] * (R(1) / R(36)), n10 = m[10] * (R(1) / R(72)), n11 = m[11] * (R(1) / R(12));
+    const R n12 = m[12] * (R(1) / R(24));
+    const R n13 = m[13] * R(0.25), n14 = m[14] * R(0.25), n15 = m[15] * R(0.25);
+    const R n16 = m[16] * R(0.125), n17 = m[17] * R(0.125), n18 = m[18] * R(0.125);
     f[0] = n0 - R(30) * n1 + R(12) * n2;
     const R be = n0 - R(11) * n1 - R(4) * n2;  // axis directions
     const R bd = n0 + R(8) * n1 + n2;           // diagonal directions

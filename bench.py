@@ -169,6 +169,7 @@ def run_ours(args) -> None:
             import torch.distributed as dist
             dist.barrier()
 
+    tile = s.autotune() if args.scheme == "fused" else None
     # warm-up (includes graph capture)
     s.step(args.warmup)
     s.sync()
@@ -279,7 +280,7 @@ def run_ours(args) -> None:
             "data": "synthetic (seeded droplet initial field, no dataset)",
             "config": {"workload": wl["name"], "grid": [wl["dx"], wl["dy"], wl["dz"]],
                        "scheme": args.scheme, "storage": args.storage, "model": wl["model"],
-                       "tr": wl["tr"], "tile": None, "parallelism": f"replicas{ws}",
+                       "tr": wl["tr"], "tile": tile, "parallelism": f"replicas{ws}",
                        "l2": "state larger than L2 (no flush needed)" if n * 44 > 129e6
                              else "state fits in L2; numbers are L2-resident"},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline, "e2e": e2e,

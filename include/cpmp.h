@@ -188,6 +188,19 @@ cpmp_status cpmp_coexistence(int model, double tr, double eos_a, double eos_b, d
                              const char *cocurve_dir, double *den_g, double *den_l, double *A,
                              double *B, double *Tc, double *Rc);
 
+/* Tile autotuner for the FUSED scheme (no reference counterpart: the
+ * reference's launch shape is fixed at 64-thread 1-D blocks, FluidCuda.cu:113).
+ * Times every instantiated (TY, TZ) column tile and x-march length on a scratch
+ * copy of the current state (the state itself is not advanced) and keeps the
+ * fastest for subsequent steps.  Outputs may be NULL.  PLAIN handles return
+ * CPMP_OK without change. */
+cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, double *ms_per_step);
+
+/* Sets the FUSED kernel's column tile (tile_y x tile_z nodes) and x-march
+ * length explicitly (no reference counterpart).  CPMP_ERR_UNSUPPORTED when the
+ * tile is not instantiated or does not fit the device's shared memory. */
+cpmp_status cpmp_set_tile(cpmp_handle *h, int tile_y, int tile_z, int march_x);
+
 /* The CUDA stream the handle launches on (cudaStream_t). */
 void *cpmp_stream(cpmp_handle *h);
 

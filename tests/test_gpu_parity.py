@@ -72,7 +72,7 @@ def test_plain_fp64_matches_reference_kernels(cpmp, case):
     s = solver_for(cpmp, kw, den=(float(z["den_g"]), float(z["den_l"])))
     fluid = z["type"] == 1
     assert np.array_equal(s.get("type"), z["type"])
-    assert rel_err(s.get("rho"), z["init_dens"], fluid) < 1e-15
+    assert rel_err(s.get("rho"), z["init_dens"], fluid) < 1e-14  # tanh: CUDA vs glibc differ by a few ulp
     s.step(int(z["steps"]))
     assert rel_err(s.get("rho"), z["dens"], fluid) < 1e-11
     u = s.get("u")
@@ -154,7 +154,9 @@ def test_mass_conservation(cpmp, scheme, storage):
     m0 = s.reduce()["mass"]
     s.step(300)
     m1 = s.reduce()["mass"]
-    tol = {"f64": 1e-12, "f32": 2e-6, "f16": 2e-4, "bf16": 2e-3}[storage]
+    # FP32 rounding is systematic in a near-steady state (the same error every
+    # step), so the drift grows linearly; FP64 shows the exact conservation.
+    tol = {"f64": 1e-12, "f32": 1e-5, "f16": 2e-4, "bf16": 2e-3}[storage]
     assert abs(m1 - m0) <= tol * m0, (m0, m1)
     s.close()
 
@@ -168,6 +170,33 @@ def test_step_chunking_is_invisible(cpmp):
         b.step(1)
     assert np.array_equal(a.get("rho"), b.get("rho"))
     assert np.array_equal(a.get("dist"), b.get("dist"))
+
+
+@pytest.mark.parametrize("storage", ["f16", "f32"])
+def test_fused_result_is_independent_of_tile(cpmp, storage):
+    """The in-kernel density of tile-interior nodes and the density pass use
+    the same decode and summation order, so any tile gives the same bits."""
+    cfg = dict(dx=48, dy=24, dz=40, radius=9.0, width=4.0, base_pt=-0.04)
+    runs = []
+    for ty, tz, xl in ((8, 32, 16), (4, 32, 7), (1, 128, 48), (2, 64, 5)):
+        s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
+        s.set_tile(ty, tz, xl)
+        s.step(12)
+        runs.append((s.get("rho"), s.get("dist")))
+        s.close()
+    for r, d in runs[1:]:
+        assert np.array_equal(r, runs[0][0])
+        assert np.array_equal(d, runs[0][1])
+
+
+def test_autotune_keeps_the_state(cpmp):
+    s = solver_for(cpmp, WALLED, scheme="fused", storage="f16")
+    s.step(3)
+    before = s.get("dist")
+    t = s.autotune()
+    assert t["tile_y"] > 0 and t["march_x"] > 0 and t["collide_ms"] > 0
+    assert np.array_equal(s.get("dist"), before)
+    s.close()
 
 
 def test_contact_angle_on_device_matches_oracle(cpmp, oracle_mod):
