@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cpmp.h"
+#include "cpmp.h"
 #include "eos.h"
 #include "kernels.h"
 

@@ -15,7 +15,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/cpmp.h"
+#include "cpmp.h"
 
 namespace cpmp {
 

@@ -2,7 +2,7 @@
 #include "k_fused.cuh"
 #include "k_plain.cuh"  // k_wall_pass
 #include "kernels.h"
-#include "../../include/cpmp.h"
+#include "cpmp.h"
 
 namespace cpmp {
 
