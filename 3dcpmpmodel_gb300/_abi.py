@@ -83,6 +83,8 @@ SIGNATURES = {
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double), C.c_int]),
     "cpmp_launch_count": (C.c_longlong, [C.c_void_p]),
+    "cpmp_mass_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
+                                    C.c_void_p]),
     "cpmp_last_error": (C.c_char_p, []),
 }
 

@@ -290,6 +290,8 @@ extern "C" {
 
 const char *cpmp_last_error(void) { return g_err.c_str(); }
 
+void cpmp_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
+
 void cpmp_params_default(cpmp_params *p)
 {
     if (!p) return;

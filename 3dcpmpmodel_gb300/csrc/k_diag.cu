@@ -5,7 +5,10 @@
 // then shared memory, in a fixed order, so results are run-to-run identical.
 #include <cfloat>
 #include <climits>
+#include <mutex>
+#include <string>
 
+#include "cpmp.h"
 #include "kernels.h"
 
 namespace cpmp {
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(kRedThreads) k_mass_partial(const uint8_t *__r
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__restrict__ part, int nb,
-                                                           double *__restrict__ out)
+                                                           double *__restrict__ out, int take_sqrt)
 {
     __shared__ double ss[kRedThreads], sm[kRedThreads], sb[kRedThreads];
     double s = 0.0, mx = 0.0, b = 0.0;
@@ -123,7 +126,7 @@ __global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__rest
     }
     if (threadIdx.x == 0) {
         out[0] = ss[0];
-        out[1] = sm[0];
+        out[1] = take_sqrt ? sqrt(sm[0]) : sm[0];
         out[2] = sb[0];
     }
 }
@@ -134,7 +137,7 @@ void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long 
 {
     const int nb = diag_partial_blocks(n);
     k_mass_partial<R><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, partials);
-    k_mass_final<<<1, kRedThreads, 0, st>>>(partials, nb, out);
+    k_mass_final<<<1, kRedThreads, 0, st>>>(partials, nb, out, 0);
 }
 
 // --------------------------------------------------------- contact angle ----
@@ -319,6 +322,74 @@ void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const
 {
     k_mv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(type, rho, u, F, mv, n);
 }
+
+// ------------------------------------------------- no-allocation variant ----
+// Partials of cpmp_mass_noalloc live in this file-scope device array instead
+// of a buffer the handle allocates.  Host code cannot use the array's name as
+// an address (it is a host-side stand-in); the device address is fetched with
+// cudaGetSymbolAddress once per device, with that device current, and cached.
+// Each call writes every partial triple it later reads, so nothing has to be
+// cleared between calls; calls that overlap on the GPU share the array and
+// race.
+static __device__ __align__(256) double g_noalloc_partials[3 * kMaxRedBlocks];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[kMaxDevices] = {nullptr};
+
+cudaError_t noalloc_partials(double **out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+}  // namespace cpmp
+
+extern "C" cpmp_status cpmp_mass_noalloc(const uint8_t *type, const float *rho, const float *mv, long long n,
+                                         void *stream, double *out)
+{
+    using namespace cpmp;
+    if (!type || !rho || !out) {
+        cpmp_internal_set_error("cpmp_mass_noalloc: null type, rho or out pointer");
+        return CPMP_ERR_PARAM;
+    }
+    if (n < 1 || n > CPMP_NOALLOC_MAX_NODES) {
+        cpmp_internal_set_error("cpmp_mass_noalloc: n must lie in [1, CPMP_NOALLOC_MAX_NODES = 2^34]");
+        return CPMP_ERR_SIZE;
+    }
+    double *part = nullptr;
+    cudaError_t e = noalloc_partials(&part);
+    if (e != cudaSuccess) {
+        cpmp_internal_set_error((std::string("cpmp_mass_noalloc: cudaGetSymbolAddress: ") +
+                                 cudaGetErrorString(e)).c_str());
+        return CPMP_ERR_CUDA;
+    }
+    const int nb = diag_partial_blocks(n);  // <= the array's kMaxRedBlocks triples
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_mass_partial<float><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, part);
+    k_mass_final<<<1, kRedThreads, 0, st>>>(part, nb, out, 1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        cpmp_internal_set_error((std::string("cpmp_mass_noalloc: launch: ") + cudaGetErrorString(e)).c_str());
+        return CPMP_ERR_CUDA;
+    }
+    return CPMP_OK;
+}
+
+namespace cpmp {
 
 template void diag_launch_mass<float>(const uint8_t *, const float *, const float *, long long, double *, double *, cudaStream_t);
 template void diag_launch_mass<double>(const uint8_t *, const double *, const double *, long long, double *, double *, cudaStream_t);

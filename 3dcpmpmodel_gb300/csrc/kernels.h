@@ -7,6 +7,9 @@
 #include "launch.h"
 #include "lbm_core.cuh"
 
+// Sets the calling thread's cpmp_last_error() message (api.cpp).
+extern "C" void cpmp_internal_set_error(const char *msg);
+
 namespace cpmp {
 
 // ---- PLAIN scheme (k_plain_f32.cu, k_plain_f64.cu) ------------------------

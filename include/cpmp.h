@@ -215,6 +215,32 @@ int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, d
 /* Number of the library's own kernel launches issued so far by this handle. */
 long long cpmp_launch_count(cpmp_handle *h);
 
+/* Largest node count cpmp_mass_noalloc accepts (the library's grid limit). */
+#define CPMP_NOALLOC_MAX_NODES (1LL << 34)
+
+/* Mass / max-speed / non-finite reduction that allocates nothing.  No
+ * counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc -- code running inside a host or framework that owns device
+ * memory, or stream-ordered pipelines where an allocation would synchronise
+ * the device -- and that hold the fields themselves: type (N bytes, FLUID =
+ * 1), rho (N floats) and, optionally, mv (3N floats, x then y then z blocks),
+ * all device pointers in the reference's node layout.  It launches on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and writes three
+ * doubles to the device pointer `out`: the FP64 sum of rho over fluid nodes,
+ * max |mv| (0 when mv is NULL) and 1.0 if a fluid density is NaN or negative
+ * (else 0.0) -- the same deterministic reduction, in the same order, as
+ * cpmp_reduce.  Its block partials live in a fixed 24 KB device array inside
+ * the library (1024 partial triples; every GPU that loads the library holds
+ * it until the process exits), so every n from 1 to CPMP_NOALLOC_MAX_NODES
+ * fits and larger n is rejected with CPMP_ERR_SIZE.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress, no
+ * allocation); make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (e.g. on two streams at once)
+ * race and give wrong results; each call writes every partial it reads, so
+ * nothing carries over between calls that follow one another. */
+cpmp_status cpmp_mass_noalloc(const uint8_t *type, const float *rho, const float *mv, long long n,
+                              void *stream, double *out);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *cpmp_last_error(void);
 
