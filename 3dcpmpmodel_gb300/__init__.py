@@ -20,7 +20,7 @@ from . import _abi
 from ._abi import (CPMP_F32, CPMP_F64, FIELD, MODEL, SCHEME, STORE, WALL, CpmpError,
                    Diag, Droplet, Params, lib)
 
-__all__ = ["Solver", "Params", "Droplet", "Diag", "CpmpError", "lib", "default_params",
+__all__ = ["Solver", "Batch", "Params", "Droplet", "Diag", "CpmpError", "lib", "default_params",
            "coexistence", "MODEL", "SCHEME", "STORE", "WALL", "FIELD", "reference_ts"]
 
 Q = 19
@@ -67,13 +67,17 @@ def coexistence(model: int, tr: float, eos_a=0.0, eos_b=0.0, eos_omega=0.0, cocu
 class Solver:
     """One simulation box on one GPU (a cpmp_handle)."""
 
-    def __init__(self, params: Params | None = None, **kw):
+    def __init__(self, params: Params | None = None, _borrowed=None, **kw):
+        self._owned = _borrowed is None
         self.params = params if params is not None else default_params(**kw)
         if params is not None and kw:
             raise TypeError("give either a Params or keyword overrides")
         self._lib = lib()
         self._h = C.c_void_p()
-        _abi.check(self._lib.cpmp_create(C.byref(self.params), C.byref(self._h)))
+        if _borrowed is None:
+            _abi.check(self._lib.cpmp_create(C.byref(self.params), C.byref(self._h)))
+        else:
+            self._h = _borrowed
         p = self.params
         self.dx, self.dy, self.dz = p.dx, p.dy, p.dz
         self.n = p.dx * p.dy * p.dz
@@ -85,9 +89,9 @@ class Solver:
 
     # life cycle -----------------------------------------------------------------
     def close(self):
-        if getattr(self, "_h", None) and self._h.value:
+        if getattr(self, "_h", None) and self._h.value and getattr(self, "_owned", True):
             self._lib.cpmp_destroy(self._h)
-            self._h = C.c_void_p()
+        self._h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -190,3 +194,70 @@ class Solver:
     @property
     def launch_count(self) -> int:
         return int(self._lib.cpmp_launch_count(self._h))
+
+
+class Batch:
+    """Many independent boxes stepped by one persistent launch (cpmp_batch).
+
+    ``boxes[i]`` is a borrowed ``Solver`` view of box i for initialisation,
+    field access and reductions; step the whole batch with ``step``."""
+
+    def __init__(self, params_list):
+        self._lib = lib()
+        arr = (Params * len(params_list))(*params_list)
+        self._b = C.c_void_p()
+        _abi.check(self._lib.cpmp_batch_create(arr, len(params_list), C.byref(self._b)))
+        self.boxes = []
+        for i, p in enumerate(params_list):
+            h = C.c_void_p()
+            _abi.check(self._lib.cpmp_batch_handle(self._b, i, C.byref(h)))
+            self.boxes.append(Solver(params=p, _borrowed=h))
+        self.nodes = int(self._lib.cpmp_batch_nodes(self._b))
+
+    def step(self, n: int = 1):
+        _abi.check(self._lib.cpmp_batch_step(self._b, int(n)))
+        return self
+
+    def sync(self):
+        _abi.check(self._lib.cpmp_batch_sync(self._b))
+
+    def set_tile(self, tile_y: int, tile_z: int, march_x: int):
+        _abi.check(self._lib.cpmp_batch_set_tile(self._b, int(tile_y), int(tile_z), int(march_x)))
+
+    def autotune(self) -> dict:
+        ty, tz, xl, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _abi.check(self._lib.cpmp_batch_autotune(self._b, C.byref(ty), C.byref(tz), C.byref(xl),
+                                                 C.byref(ms)))
+        return {"tile_y": ty.value, "tile_z": tz.value, "march_x": xl.value, "step_ms": ms.value}
+
+    @property
+    def stream(self) -> int:
+        return self._lib.cpmp_batch_stream(self._b) or 0
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._lib.cpmp_batch_launch_count(self._b))
+
+    def kernel_timing(self, on: bool):
+        _abi.check(self._lib.cpmp_batch_set_kernel_timing(self._b, 1 if on else 0))
+
+    def kernel_times(self) -> dict:
+        cap = 16
+        names = (C.c_char_p * cap)()
+        launches = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        k = self._lib.cpmp_batch_kernel_times(self._b, names, launches, ms, cap)
+        return {names[i].decode(): (launches[i], ms[i]) for i in range(min(k, cap))}
+
+    def close(self):
+        if getattr(self, "_b", None) and self._b.value:
+            for s in self.boxes:
+                s._h = C.c_void_p()
+            self._lib.cpmp_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -83,6 +83,21 @@ SIGNATURES = {
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double), C.c_int]),
     "cpmp_launch_count": (C.c_longlong, [C.c_void_p]),
+    "cpmp_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "cpmp_batch_handle": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "cpmp_batch_count": (C.c_int, [C.c_void_p]),
+    "cpmp_batch_nodes": (C.c_longlong, [C.c_void_p]),
+    "cpmp_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "cpmp_batch_sync": (C.c_int, [C.c_void_p]),
+    "cpmp_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "cpmp_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "cpmp_batch_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "cpmp_batch_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_double), C.c_int]),
+    "cpmp_batch_launch_count": (C.c_longlong, [C.c_void_p]),
+    "cpmp_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "cpmp_batch_destroy": (None, [C.c_void_p]),
     "cpmp_mass_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p,
                                     C.c_void_p]),
     "cpmp_last_error": (C.c_char_p, []),

@@ -64,6 +64,22 @@ struct cpmp_handle {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
     int launches_per_step = 0;
+    bool in_batch = false;       // stepped by its cpmp_batch, on the batch's stream
+};
+
+struct cpmp_batch {
+    std::vector<cpmp_handle *> boxes;
+    cudaStream_t st = nullptr;
+    int device = 0, storage = 0, lap_order = 5, wall_mode = 1, complex_bc = 1;
+    FusedTile tile{8, 32, 16};
+    KParams<float> *d_params = nullptr;
+    BatchBox *d_boxes = nullptr;
+    unsigned *d_counter = nullptr;
+    long long total_items = 0, nodes = 0, max_cols = 0, launches = 0;
+    int max_dx = 0;
+    cudaGraphExec_t gexec = nullptr;
+    std::unique_ptr<LaunchHook> hook;
+    bool timing = false;
 };
 
 namespace {
@@ -443,6 +459,7 @@ void cpmp_destroy(cpmp_handle *h)
     if (!h) return;
     cudaSetDevice(h->p.device);
     if (h->st) cudaStreamSynchronize(h->st);
+    if (h->in_batch) h->st = nullptr;  // the batch owns the stream
     h->hook.reset();
     free_all(h);
     delete h;
@@ -504,6 +521,7 @@ cpmp_status cpmp_step(cpmp_handle *h, int nsteps)
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
     if (nsteps < 0) return fail(CPMP_ERR_PARAM, "nsteps must be >= 0");
     if (!h->initialised) return fail(CPMP_ERR_PARAM, "cpmp_init_droplet or cpmp_set_field(DIST) first");
+    if (h->in_batch) return fail(CPMP_ERR_PARAM, "boxes of a batch are stepped with cpmp_batch_step");
     CK(cudaSetDevice(h->p.device));
     LaunchHook *hook = h->timing ? h->hook.get() : nullptr;
     int left = nsteps;
@@ -843,5 +861,370 @@ int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, d
 }
 
 long long cpmp_launch_count(cpmp_handle *h) { return h ? h->launches : 0; }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batches --
+namespace {
+
+cpmp_status batch_upload(cpmp_batch *b)
+{
+    const int nb = (int)b->boxes.size();
+    std::vector<KParams<float>> kp(nb);
+    std::vector<BatchBox> bx(nb);
+    long long item = 0;
+    b->nodes = 0;
+    b->max_dx = 0;
+    b->max_cols = 0;
+    for (int i = 0; i < nb; ++i) {
+        cpmp_handle *h = b->boxes[i];
+        kp[i] = make_kparams<float>(h);
+        const bool even = (h->step & 1) == 0;
+        bx[i].h = h->h;
+        bx[i].f0[0] = h->f0[0];
+        bx[i].f0[1] = h->f0[1];
+        bx[i].rho[0] = (float *)(even ? h->rho : h->rho2);
+        bx[i].rho[1] = (float *)(even ? h->rho2 : h->rho);
+        bx[i].tiles_z = (h->p.dz + b->tile.tz - 1) / b->tile.tz;
+        bx[i].tiles_y = (h->p.dy + b->tile.ty - 1) / b->tile.ty;
+        bx[i].item0 = item;
+        item += (long long)bx[i].tiles_z * bx[i].tiles_y * ((h->p.dx + b->tile.xl - 1) / b->tile.xl);
+        b->nodes += h->n;
+        b->max_dx = std::max(b->max_dx, h->p.dx);
+        b->max_cols = std::max(b->max_cols, (long long)h->p.dx * h->p.dy);
+    }
+    b->total_items = item;
+    CK(cudaMemcpyAsync(b->d_params, kp.data(), nb * sizeof(KParams<float>), cudaMemcpyHostToDevice, b->st));
+    CK(cudaMemcpyAsync(b->d_boxes, bx.data(), nb * sizeof(BatchBox), cudaMemcpyHostToDevice, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    return CPMP_OK;
+}
+
+void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
+{
+    const int P = (int)(b->boxes[0]->step & 1);
+    fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params, b->d_boxes,
+                     (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, P, b->d_counter, b->st, hook);
+    if (!bookkeeping) return;
+    for (cpmp_handle *h : b->boxes) {
+        h->step += 1;
+        std::swap(h->rho, h->rho2);
+    }
+    b->launches += (b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2;
+}
+
+cpmp_status batch_check(cpmp_batch *b)
+{
+    const long long s0 = b->boxes[0]->step;
+    for (cpmp_handle *h : b->boxes) {
+        if (!h->initialised) return fail(CPMP_ERR_PARAM, "initialise every box of the batch first");
+        if ((h->step & 1) != (s0 & 1)) return fail(CPMP_ERR_PARAM, "boxes of a batch must share the step parity");
+    }
+    return CPMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch **out)
+{
+    if (!params || !out || count < 1) return fail(CPMP_ERR_PARAM, "need count >= 1 parameter sets");
+    *out = nullptr;
+    const cpmp_params &p0 = params[0];
+    for (int i = 0; i < count; ++i) {
+        const cpmp_params &p = params[i];
+        if (p.scheme != CPMP_SCHEME_FUSED) return fail(CPMP_ERR_UNSUPPORTED, "batches run the FUSED scheme");
+        if (p.storage != p0.storage || p.lap_order != p0.lap_order || p.wall_mode != p0.wall_mode ||
+            p.complex_bc != p0.complex_bc || p.device != p0.device)
+            return fail(CPMP_ERR_PARAM, "boxes of a batch share storage, lap_order, wall_mode, complex_bc, device");
+    }
+    std::unique_ptr<cpmp_batch> b(new cpmp_batch());
+    b->device = p0.device;
+    b->storage = p0.storage;
+    b->lap_order = p0.lap_order;
+    b->wall_mode = p0.wall_mode;
+    b->complex_bc = p0.complex_bc;
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    auto cleanup = [&]() {
+        for (cpmp_handle *h : b->boxes) cpmp_destroy(h);
+        b->boxes.clear();
+        if (b->d_params) cudaFree(b->d_params);
+        if (b->d_boxes) cudaFree(b->d_boxes);
+        if (b->d_counter) cudaFree(b->d_counter);
+        cudaStreamDestroy(b->st);
+    };
+    for (int i = 0; i < count; ++i) {
+        cpmp_handle *h = nullptr;
+        cpmp_status s = cpmp_create(&params[i], &h);
+        if (s != CPMP_OK) {
+            cleanup();
+            return s;
+        }
+        cudaStreamDestroy(h->st);
+        h->st = b->st;
+        h->in_batch = true;
+        b->boxes.push_back(h);
+    }
+    // one tile for every box: the first box's heuristic choice, refined by cpmp_batch_autotune
+    b->tile = b->boxes[0]->tile;
+    int minx = b->boxes[0]->p.dx;
+    for (cpmp_handle *h : b->boxes) minx = std::min(minx, h->p.dx);
+    b->tile.xl = std::min(b->tile.xl, minx);
+    for (cpmp_handle *h : b->boxes) h->tile = b->tile;
+    cpmp_status s;
+    if ((s = dalloc((void **)&b->d_params, count * sizeof(KParams<float>), "batch params")) != CPMP_OK ||
+        (s = dalloc((void **)&b->d_boxes, count * sizeof(BatchBox), "batch boxes")) != CPMP_OK ||
+        (s = dalloc((void **)&b->d_counter, sizeof(unsigned), "batch counter")) != CPMP_OK) {
+        cleanup();
+        return s;
+    }
+    if ((s = batch_upload(b.get())) != CPMP_OK) {
+        cleanup();
+        return s;
+    }
+    *out = b.release();
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_handle(cpmp_batch *b, int index, cpmp_handle **h)
+{
+    if (!b || !h || index < 0 || index >= (int)b->boxes.size()) return fail(CPMP_ERR_PARAM, "box index");
+    *h = b->boxes[index];
+    return CPMP_OK;
+}
+
+int cpmp_batch_count(cpmp_batch *b) { return b ? (int)b->boxes.size() : 0; }
+
+long long cpmp_batch_nodes(cpmp_batch *b) { return b ? b->nodes : 0; }
+
+cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    if (nsteps < 0) return fail(CPMP_ERR_PARAM, "nsteps must be >= 0");
+    cpmp_status s;
+    if ((s = batch_check(b)) != CPMP_OK) return s;
+    CK(cudaSetDevice(b->device));
+    // the device tables name each box's even- and odd-step density buffers,
+    // so they stay valid whatever the parity
+    LaunchHook *hook = b->timing ? b->hook.get() : nullptr;
+    int left = nsteps;
+    if (hook || nsteps < 2) {
+        for (; left > 0; --left) batch_one_step(b, hook, true);
+        CK(cudaGetLastError());
+        return CPMP_OK;
+    }
+    if (b->boxes[0]->step & 1) {
+        batch_one_step(b, nullptr, true);
+        --left;
+    }
+    if (left >= 2) {
+        if (!b->gexec) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+            batch_one_step(b, nullptr, false);
+            // the second step of the pair runs at odd parity on the same tables
+            {
+                const int P = 1;
+                fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params,
+                                 b->d_boxes, (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, P,
+                                 b->d_counter, b->st, nullptr);
+            }
+            cudaError_t e = cudaStreamEndCapture(b->st, &g);
+            if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                b->gexec = nullptr;
+                return fail(CPMP_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+            }
+        }
+        while (left >= 2) {
+            CK(cudaGraphLaunch(b->gexec, b->st));
+            for (cpmp_handle *h : b->boxes) h->step += 2;  // two swaps: rho pointers unchanged
+            b->launches += 2LL * ((b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2);
+            left -= 2;
+        }
+    }
+    if (left == 1) batch_one_step(b, nullptr, true);
+    CK(cudaGetLastError());
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_sync(cpmp_batch *b)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->st));
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_set_tile(cpmp_batch *b, int tile_y, int tile_z, int march_x)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
+    if (!fused_tile_usable(b->storage, b->lap_order, tile_y, tile_z))
+        return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
+    b->tile = FusedTile{tile_y, tile_z, march_x};
+    for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
+    for (cpmp_handle *h : b->boxes) h->tile = b->tile;
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    return batch_upload(b);
+}
+
+cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *march_x, double *ms_per_step)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    cpmp_status s;
+    if ((s = batch_check(b)) != CPMP_OK) return s;
+    CK(cudaSetDevice(b->device));
+    // scratch copies of every box's lattice so the state is not advanced
+    const size_t hs = b->storage == CPMP_STORE_F32 ? 4 : 2;
+    std::vector<void *> scratch;
+    auto free_scratch = [&]() {
+        for (void *q : scratch) cudaFree(q);
+        scratch.clear();
+    };
+    struct Saved { void *h, *rho, *rho2; float *f0[2]; };
+    std::vector<Saved> saved;
+    for (cpmp_handle *h : b->boxes) {
+        const size_t n = (size_t)h->n;
+        void *sh = nullptr, *sa = nullptr, *sb = nullptr, *sr = nullptr, *sr2 = nullptr;
+        if ((s = dalloc(&sh, (CPMP_Q - 1) * n * hs, "tune h")) != CPMP_OK) { free_scratch(); return s; }
+        scratch.push_back(sh);
+        if ((s = dalloc(&sa, n * 4, "tune f0")) != CPMP_OK) { free_scratch(); return s; }
+        scratch.push_back(sa);
+        if ((s = dalloc(&sb, n * 4, "tune f0")) != CPMP_OK) { free_scratch(); return s; }
+        scratch.push_back(sb);
+        if ((s = dalloc(&sr, n * 4, "tune rho")) != CPMP_OK) { free_scratch(); return s; }
+        scratch.push_back(sr);
+        if ((s = dalloc(&sr2, n * 4, "tune rho")) != CPMP_OK) { free_scratch(); return s; }
+        scratch.push_back(sr2);
+        cudaMemcpyAsync(sh, h->h, (CPMP_Q - 1) * n * hs, cudaMemcpyDeviceToDevice, b->st);
+        cudaMemcpyAsync(sa, h->f0[0], n * 4, cudaMemcpyDeviceToDevice, b->st);
+        cudaMemcpyAsync(sb, h->f0[1], n * 4, cudaMemcpyDeviceToDevice, b->st);
+        cudaMemcpyAsync(sr, h->rho, n * 4, cudaMemcpyDeviceToDevice, b->st);
+        cudaMemcpyAsync(sr2, h->rho2, n * 4, cudaMemcpyDeviceToDevice, b->st);
+        saved.push_back(Saved{h->h, h->rho, h->rho2, {h->f0[0], h->f0[1]}});
+        h->h = sh;
+        h->f0[0] = (float *)sa;
+        h->f0[1] = (float *)sb;
+        h->rho = sr;
+        h->rho2 = sr2;
+    }
+    const FusedTile keep = b->tile;
+    const long long step_keep = b->boxes[0]->step;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    FusedTile best = keep;
+    double best_ms = 1e30;
+    const int xls[] = {8, 16, 32, 64};
+    cudaError_t err = cudaSuccess;
+    for (int t = 0; t < fused_tile_count() && err == cudaSuccess; ++t) {
+        for (int xi = 0; xi < 4; ++xi) {
+            FusedTile ft = fused_tile(t, xls[xi]);
+            if (!fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz)) continue;
+            b->tile = ft;
+            for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
+            if (batch_upload(b) != CPMP_OK) break;
+            batch_one_step(b, nullptr, false);
+            cudaEventRecord(e0, b->st);
+            batch_one_step(b, nullptr, false);
+            batch_one_step(b, nullptr, false);
+            cudaEventRecord(e1, b->st);
+            err = cudaEventSynchronize(e1);
+            if (err != cudaSuccess) break;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            b->launches += 3LL * ((b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2);
+            if (ms / 2 < best_ms) {
+                best_ms = ms / 2;
+                best = b->tile;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (size_t i = 0; i < b->boxes.size(); ++i) {
+        cpmp_handle *h = b->boxes[i];
+        h->h = saved[i].h;
+        h->rho = saved[i].rho;
+        h->rho2 = saved[i].rho2;
+        h->f0[0] = saved[i].f0[0];
+        h->f0[1] = saved[i].f0[1];
+        h->step = step_keep;
+    }
+    cudaStreamSynchronize(b->st);
+    free_scratch();
+    if (err != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(err));
+    b->tile = best;
+    for (cpmp_handle *h : b->boxes) h->tile = best;
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
+    if ((s = batch_upload(b)) != CPMP_OK) return s;
+    if (tile_y) *tile_y = best.ty;
+    if (tile_z) *tile_z = best.tz;
+    if (march_x) *march_x = best.xl;
+    if (ms_per_step) *ms_per_step = best_ms;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_set_kernel_timing(cpmp_batch *b, int on)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    if (on) {
+        if (!b->hook) b->hook.reset(new LaunchHook());
+        b->hook->reset();
+        b->timing = true;
+    } else {
+        if (b->hook) b->hook->fold();
+        b->timing = false;
+    }
+    return CPMP_OK;
+}
+
+int cpmp_batch_kernel_times(cpmp_batch *b, const char **names, long long *launches, double *ms, int cap)
+{
+    if (!b || !b->hook) return 0;
+    cudaSetDevice(b->device);
+    b->hook->fold();
+    int k = 0;
+    for (int c = 0; c < K_CLASSES; ++c) {
+        if (b->hook->launches[c] == 0) continue;
+        if (k < cap) {
+            if (names) names[k] = kernel_class_name(c);
+            if (launches) launches[k] = b->hook->launches[c];
+            if (ms) ms[k] = b->hook->ms[c];
+        }
+        ++k;
+    }
+    return k;
+}
+
+long long cpmp_batch_launch_count(cpmp_batch *b) { return b ? b->launches : 0; }
+
+void *cpmp_batch_stream(cpmp_batch *b) { return b ? (void *)b->st : nullptr; }
+
+void cpmp_batch_destroy(cpmp_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->st);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (cpmp_handle *h : b->boxes) cpmp_destroy(h);
+    cudaFree(b->d_params);
+    cudaFree(b->d_boxes);
+    cudaFree(b->d_counter);
+    cudaStreamDestroy(b->st);
+    b->hook.reset();
+    delete b;
+}
 
 }  // extern "C"

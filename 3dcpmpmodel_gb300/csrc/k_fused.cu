@@ -1,4 +1,6 @@
 // k_fused.cu -- FUSED scheme instantiations and launchers.
+#include <algorithm>
+
 #include "k_fused.cuh"
 #include "k_plain.cuh"  // k_wall_pass
 #include "kernels.h"
@@ -93,6 +95,19 @@ __global__ void __launch_bounds__(256) k_velocity(KParams<float> p, int P, const
     u[I + 2 * p.n] = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) / r;
 }
 
+// All boxes of a batch: blockIdx.y = box; the wall of box b at parity P is
+// computed on rho[P] and mirrored into rho[1-P].
+__global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
+                                  int pass, int P)
+{
+    const KParams<float> &p = params[blockIdx.y];
+    if (p.wall_mode != 1) return;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)p.dx * p.dy) return;
+    const BatchBox &b = boxes[blockIdx.y];
+    wall_column<float>(p, pass, c, b.rho[P], nullptr, b.rho[1 - P]);
+}
+
 // ------------------------------------------------------------- dispatch ----
 namespace {
 constexpr int kTiles[][2] = {{4, 32}, {8, 32}, {16, 32}, {2, 64}, {1, 128}};
@@ -147,6 +162,8 @@ void set_attr_t(int si, int max_smem)
     bool ok = (int)b <= max_smem;
     if (ok)
         ok = cudaFuncSetAttribute(k_fused_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)b) == cudaSuccess &&
+             cudaFuncSetAttribute(k_fused_collide_batch<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)b) == cudaSuccess;
     cudaGetLastError();
     g_usable[si][L - 2][tile_index(TY, TZ)] = ok;
@@ -240,6 +257,66 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
         k_density<S><<<g, 128, 0, st>>>(p, P, (const S *)h, f0, rho, ft);
+    });
+    hook_end(hook, K_DENSITY, st);
+}
+
+// ------------------------------------------------------------- batches ----
+namespace {
+template <class S, int TY, int TZ, int L>
+void batch_collide_t(const KParams<float> *params, const BatchBox *boxes, int nbox, long long total, int P,
+                     int xl, unsigned *counter, cudaStream_t st)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_collide_batch<S, TY, TZ, L>, TY * TZ,
+                                                  fused_smem_bytes<S, TY, TZ, L>());
+    long long grid = (long long)sms * std::max(per_sm, 1);
+    if (grid > total) grid = total;
+    if (grid < 1) grid = 1;
+    k_fused_collide_batch<S, TY, TZ, L><<<(unsigned)grid, TY * TZ, fused_smem_bytes<S, TY, TZ, L>(), st>>>(
+        params, boxes, nbox, total, P, xl, counter);
+}
+template <class S, int L>
+void batch_collide_l(const FusedTile &t, const KParams<float> *params, const BatchBox *boxes, int nbox,
+                     long long total, int P, unsigned *counter, cudaStream_t st)
+{
+    if (t.ty == 4 && t.tz == 32) batch_collide_t<S, 4, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else if (t.ty == 8 && t.tz == 32) batch_collide_t<S, 8, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else if (t.ty == 16 && t.tz == 32) batch_collide_t<S, 16, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else if (t.ty == 2 && t.tz == 64) batch_collide_t<S, 2, 64, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else batch_collide_t<S, 1, 128, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+}
+}  // namespace
+
+void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
+                      const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
+                      int max_dx, long long max_cols, int P, unsigned *counter, cudaStream_t st, LaunchHook *hook)
+{
+    if (wall_mode == 1) {
+        const dim3 gw((unsigned)((max_cols + 127) / 128), (unsigned)nbox);
+        for (int s = 0; s < (complex_bc ? 3 : 1); ++s) {
+            hook_begin(hook, K_WALL, st);
+            k_wall_pass_batch<<<gw, 128, 0, st>>>(params, boxes, s, P);
+            hook_end(hook, K_WALL, st);
+        }
+    }
+    hook_begin(hook, K_FUSED, st);
+    cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        if (lap_order == 7)
+            batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
+        else
+            batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
+    });
+    hook_end(hook, K_FUSED, st);
+    hook_begin(hook, K_DENSITY, st);
+    const FoldTile ft{t.ty, t.tz, t.xl};
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        k_density_batch<S><<<dim3((unsigned)max_dx, (unsigned)nbox), 256, 0, st>>>(params, boxes, 1 - P, ft);
     });
     hook_end(hook, K_DENSITY, st);
 }

@@ -147,13 +147,11 @@ __device__ __forceinline__ bool fold_interior(const KParams<float> &p, const Fol
 // FluidCuda.cu:357-361) on fluid nodes: r = f0, then r += f_q for q = 1..18
 // in order, every term decoded by decode_pop.  Grid: (z blocks, dy, dx).
 template <class S>
-__global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const S *__restrict__ h,
-                                                 const float *__restrict__ f0, float *__restrict__ rho,
-                                                 FoldTile fold)
+__device__ __forceinline__ void density_node(const KParams<float> &p, int P, const S *__restrict__ h,
+                                             const float *__restrict__ f0, float *__restrict__ rho,
+                                             const FoldTile &fold, int i, int j, int k)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, i = blockIdx.z;
-    if (k >= p.dz || solid_k(p.wall_mode, k, p.dz)) return;
+    if (solid_k(p.wall_mode, k, p.dz)) return;
     if (fold_interior(p, fold, i, j, k)) return;
     const int plane = p.dy * p.dz;
     const long long I = ((long long)i * p.dy + j) * p.dz + k;
@@ -177,6 +175,16 @@ __global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const 
 #pragma unroll
     for (int q = 1; q < Q; ++q) r = __fadd_rn(r, f[q]);
     rho[I] = r;
+}
+
+template <class S>
+__global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const S *__restrict__ h,
+                                                 const float *__restrict__ f0, float *__restrict__ rho,
+                                                 FoldTile fold)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= p.dz) return;
+    density_node<S>(p, P, h, f0, rho, fold, blockIdx.z, blockIdx.y, k);
 }
 
 // --------------------------------------------------------- fused step ----
@@ -241,16 +249,16 @@ __device__ __forceinline__ int mod_small(int t, int m)
 // F = -rho grad7(mu) + grad7(rho)/3, decodes its populations, collides (MRT +
 // exact-difference forcing) and streams A-A in place.
 template <class S, int TY, int TZ, int L>
-__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
-    k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
-                    float *__restrict__ f0n, const float *__restrict__ rho, float *__restrict__ rho_next,
-                    int xl)
+__device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__restrict__ h,
+                                           const float *__restrict__ f0c, float *__restrict__ f0n,
+                                           const float *__restrict__ rho, float *__restrict__ rho_next,
+                                           const int z0, const int y0, const int x0, const int xl,
+                                           float4 *smem4)
 {
     using G = FusedGeom<TY, TZ, L>;
     constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
     constexpr int AY = G::AY, AZ = G::AZ;
     constexpr int NT = TY * TZ;
-    extern __shared__ float4 smem4[];
     float *srho = reinterpret_cast<float *>(smem4);
     float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
     float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
@@ -263,8 +271,6 @@ __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
     auto pc_f0 = [&](int slot) { return reinterpret_cast<float *>(pc_h(slot) + 18 * NTILE); };
 
     const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
-    const int z0 = blockIdx.x * TZ, y0 = blockIdx.y * TY;
-    const int x0 = blockIdx.z * xl;
     const int x1 = min(x0 + xl, p.dx);
     const int plane = p.dy * p.dz;
     const long long n = p.n;
@@ -535,6 +541,77 @@ __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
     __syncthreads();
     if (x1 - 2 >= x0 + 1) fold_density(x1 - 2);
     cp_async_wait_all();
+}
+
+// One box: CTA (bx, by, bz) owns z tile bx, y tile by and x chunk bz.
+template <class S, int TY, int TZ, int L>
+__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
+    k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
+                    float *__restrict__ f0n, const float *__restrict__ rho, float *__restrict__ rho_next,
+                    int xl)
+{
+    extern __shared__ float4 smem4[];
+    fused_tile<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, rho_next, blockIdx.x * TZ, blockIdx.y * TY,
+                             blockIdx.z * xl, xl, smem4);
+}
+
+// Many boxes in one persistent launch: each CTA takes (box, z tile, y tile,
+// x chunk) work items from an atomic counter until none are left.  Uneven
+// box sizes balance themselves; every box shares the tile shape and march.
+template <class S, int TY, int TZ, int L>
+__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
+    k_fused_collide_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
+                          int nbox, long long total_items, int P, int xl, unsigned int *counter)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ long long item_s;
+    __shared__ int box_s;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = (long long)atomicAdd(counter, 1u);
+            int lo = 0, hi = nbox - 1;
+            while (lo < hi) {  // last box with item0 <= it
+                const int mid = (lo + hi + 1) / 2;
+                if (boxes[mid].item0 <= it) lo = mid;
+                else hi = mid - 1;
+            }
+            item_s = it;
+            box_s = lo;
+        }
+        __syncthreads();
+        const long long it = item_s;
+        if (it >= total_items) break;
+        const BatchBox &bx = boxes[box_s];
+        const KParams<float> &p = params[box_s];
+        const long long local = it - bx.item0;
+        const int per_chunk = bx.tiles_z * bx.tiles_y;
+        const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
+        const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
+        fused_tile<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], bx.rho[1 - P],
+                                 ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
+        __syncthreads();
+    }
+}
+
+// Batched density pass: one block per (box, x plane), threads over the plane.
+template <class S>
+__global__ void __launch_bounds__(256) k_density_batch(const KParams<float> *__restrict__ params,
+                                                       const BatchBox *__restrict__ boxes, int P,
+                                                       FoldTile fold)
+{
+    const int b = blockIdx.y;
+    const KParams<float> &p = params[b];
+    const int i = blockIdx.x;
+    if (i >= p.dx) return;
+    const BatchBox &bx = boxes[b];
+    const S *h = (const S *)bx.h;
+    const float *f0 = bx.f0[P];
+    float *rho = bx.rho[P];
+    const int nplane = p.dy * p.dz;
+    for (int e = threadIdx.x; e < nplane; e += blockDim.x) {
+        const int j = e / p.dz, k = e - j * p.dz;
+        density_node<S>(p, P, h, f0, rho, fold, i, j, k);
+    }
 }
 
 template <class S, int TY, int TZ, int L>

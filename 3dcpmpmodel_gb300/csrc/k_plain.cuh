@@ -83,10 +83,8 @@ __device__ __forceinline__ R wall_extrap(const KParams<R> &p, const R *rho, int 
 }
 
 template <class R>
-__global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu, R *mirror = nullptr)
+__device__ __forceinline__ void wall_column(const KParams<R> &p, int pass, long long c, R *rho, R *mu, R *mirror)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= (long long)p.dx * p.dy) return;
     const int i = (int)(c / p.dy), j = (int)(c % p.dy);
     const int D = p.dz;
     if (pass == 0) {
@@ -120,6 +118,15 @@ __global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu, R *mirror = n
         }
     }
 }
+
+template <class R>
+__global__ void k_wall_pass(KParams<R> p, int pass, R *rho, R *mu, R *mirror = nullptr)
+{
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long long)p.dx * p.dy) return;
+    wall_column<R>(p, pass, c, rho, mu, mirror);
+}
+
 
 // ------------------------------------------------------------- stencils ----
 // 4th-order 13-point Laplacian (GradD5, Common.h:189-192) and the 6th-order

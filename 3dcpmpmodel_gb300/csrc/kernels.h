@@ -63,6 +63,14 @@ void fused_launch_collide(int storage, const KParams<float> &p, int P, const Fus
 // the nodes the fused collide with that tile already wrote are skipped.
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
                           const float *f0, float *rho, const FusedTile *fold, cudaStream_t st, LaunchHook *hook);
+// One time step of every box of a batch: batched wall passes, the persistent
+// fused collide over all (box, tile, chunk) work items, the batched density
+// pass.  params/boxes are device arrays of nbox entries; counter is one
+// device unsigned (reset here); max_dx / max_cols bound the boxes' x extent
+// and wall columns.
+void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
+                      const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
+                      int max_dx, long long max_cols, int P, unsigned *counter, cudaStream_t st, LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).
 void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,

@@ -98,6 +98,16 @@ inline void hook_end(LaunchHook *h, int cls, cudaStream_t st)
     if (h->pending.size() > 4096) h->fold();
 }
 
+// Buffers of one box of a batch (the KParams of every box live in a device
+// array next to these).
+struct BatchBox {
+    void *h;
+    float *f0[2];
+    float *rho[2];         // rho[0] is the density read at even steps
+    long long item0;       // first collide work item of this box
+    int tiles_z, tiles_y;  // column tiles per x plane
+};
+
 // Initial droplet (SetFlowField, FluidCuda.cu:199-241).
 struct DropletDev {
     double cx, cy, cz, radius, width, den_g, den_l;

@@ -40,6 +40,7 @@ WORKLOADS = {
     "c2": dict(name="wetting_128x128x96_prw", dx=128, dy=128, dz=96, model=202, tr=0.7,
                radius=30.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8,
                centre=(64.0, 64.0, 3.0)),
+    "c4": dict(name="batched_96_boxes_48to112cube_fp16", batch=96, seed=0),
     "c1": dict(name="periodic_64cube_cs", dx=64, dy=64, dz=64, model=206, tr=0.85, eos_a=0.5,
                eos_b=4.0, radius=16.0, width=2.0, wall_mode=0, base_pt=0.0, k=0.2, ka=0.01,
                tau=1.0, centre=(32.0, 32.0, 32.0)),
@@ -160,6 +161,9 @@ def run_ours(args) -> None:
     importlib.import_module("3dcpmpmodel_gb300.build").build()
     cp = importlib.import_module("3dcpmpmodel_gb300")
     wl = WORKLOADS[args.workload]
+    if "batch" in wl:
+        run_batch(args, wl, cp, torch)
+        return
     s = make_solver(cp, wl, args.scheme, args.storage, local)
     n = s.n
     stream = torch.cuda.ExternalStream(s.stream)
@@ -291,6 +295,81 @@ def run_ours(args) -> None:
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def c4_params(cp, storage: str, seed: int = 0, count: int = 96):
+    """96 droplet-on-wall boxes: cube edge uniform in 48..112, EOS drawn from
+    VdW / CS / PR, T/Tc uniform in 0.6-0.9 snapped to the 0.005 table grid,
+    wall potential in the range the reference calibrates to 30-150 degrees
+    (FluidCuda.cu:128), FP16 storage; seeded."""
+    rng = np.random.default_rng(seed)
+    out, drops = [], []
+    for _ in range(count):
+        L = int(rng.integers(48, 113))
+        model = int(rng.choice([201, 206, 202]))
+        tr = round(float(rng.uniform(0.6, 0.9)) / 0.005) * 0.005
+        base_pt = float(rng.uniform(-0.06, 0.15))
+        p = cp.default_params(dx=L, dy=L, dz=L, model=model, tr=tr, base_pt=base_pt,
+                              scheme=cp.SCHEME["fused"], storage=cp.STORE[storage])
+        out.append(p)
+        drops.append(dict(radius=L / 4, width=5.0, centre=(L / 2, L / 2, 3.0)))
+    return out, drops
+
+
+def run_batch(args, wl: dict, cp, torch) -> None:
+    params, drops = c4_params(cp, args.storage, wl["seed"], wl["batch"])
+    b = cp.Batch(params)
+    for s, d in zip(b.boxes, drops):
+        s.set_flow_field(**d)
+    tile = b.autotune()
+    stream = torch.cuda.ExternalStream(b.stream)
+    b.step(args.warmup)
+    b.sync()
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    l0 = b.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    b.sync()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    launches = b.launch_count - l0
+    value = b.nodes * args.steps / (ms / 1e3) / 1e6
+    b.kernel_timing(True)
+    b.step(args.steps)
+    b.sync()
+    kt = b.kernel_times()
+    b.kernel_timing(False)
+    bytes_per = algorithmic_bytes("fused", args.storage)
+    dom_name, (dom_launches, dom_ms) = max(kt.items(), key=lambda kv: kv[1][1])
+    alg = bytes_per.get(dom_name, bytes_per["step"])
+    achieved = alg * b.nodes / (dom_ms / dom_launches / 1e3) / 1e9
+    peaks = measured_peaks()
+    bad = sum(1 for s in b.boxes if s.reduce(allow_nonfinite=True)["nonfinite"])
+    line = {
+        "metric": METRIC + " (aggregate over a batch)", "value": round(value, 1), "unit": "MLUPS",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 arithmetic, " + args.storage + " population storage",
+        "data": "synthetic (seeded droplet initial fields, no dataset)",
+        "config": {"workload": wl["name"], "boxes": len(params), "total_nodes": b.nodes,
+                   "tile": tile, "parallelism": "one persistent launch per step",
+                   "l2": "state larger than L2" if b.nodes * 44 > 129e6 else "state fits in L2",
+                   "boxes_nonfinite": bad},
+        "gpu_launches": launches, "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "peak_source": peaks["source"], "traffic": None, "alg_bytes_per_lu": alg,
+                     "kernels_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in kt.items()}},
+        "e2e": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line))
+    b.close()
 
 
 def cpu_sample(args, wl: dict) -> dict:

@@ -215,6 +215,39 @@ int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, d
 /* Number of the library's own kernel launches issued so far by this handle. */
 long long cpmp_launch_count(cpmp_handle *h);
 
+/* ---- Batches: many independent boxes stepped by one persistent launch ----
+ * No reference counterpart (the reference runs one box per process).  All
+ * boxes use the FUSED scheme and share storage, lap_order, wall_mode,
+ * complex_bc and device; grid, EOS model, T/Tc, K, kappa, rates and wall
+ * potential may differ per box.  Each time step is three batched wall
+ * passes, ONE persistent fused-collide launch whose CTAs take (box, tile,
+ * x-chunk) work items from a device counter until none are left, and one
+ * batched density pass; cpmp_batch_step replays two steps as a CUDA graph. */
+typedef struct cpmp_batch cpmp_batch;
+
+/* Creates count boxes from params[count] (every box an ordinary handle that
+ * shares the batch's stream). */
+cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch **out);
+/* Box `index` as a handle for cpmp_init_droplet, cpmp_set_base_pt,
+ * cpmp_set_wall_field, cpmp_get_field, cpmp_set_field, cpmp_reduce.  The batch
+ * owns it: do not cpmp_destroy or cpmp_step it (cpmp_step returns
+ * CPMP_ERR_PARAM for batch boxes). */
+cpmp_status cpmp_batch_handle(cpmp_batch *b, int index, cpmp_handle **h);
+int cpmp_batch_count(cpmp_batch *b);
+long long cpmp_batch_nodes(cpmp_batch *b);   /* total lattice nodes of all boxes */
+/* nsteps time steps of every box (asynchronous on the batch stream). */
+cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps);
+cpmp_status cpmp_batch_sync(cpmp_batch *b);
+/* Tile shape / x-march shared by all boxes; the autotuner times the
+ * candidates on scratch copies of every box (the state is not advanced). */
+cpmp_status cpmp_batch_set_tile(cpmp_batch *b, int tile_y, int tile_z, int march_x);
+cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *march_x, double *ms_per_step);
+cpmp_status cpmp_batch_set_kernel_timing(cpmp_batch *b, int on);
+int cpmp_batch_kernel_times(cpmp_batch *b, const char **names, long long *launches, double *ms, int cap);
+long long cpmp_batch_launch_count(cpmp_batch *b);
+void *cpmp_batch_stream(cpmp_batch *b);
+void cpmp_batch_destroy(cpmp_batch *b);
+
 /* Largest node count cpmp_mass_noalloc accepts (the library's grid limit). */
 #define CPMP_NOALLOC_MAX_NODES (1LL << 34)
 
