@@ -403,7 +403,9 @@ def cpu_sample(args, wl: dict) -> dict:
               wall_mode=wl["wall_mode"])
     if "eos_a" in wl:
         kw["eos_a"], kw["eos_b"] = wl["eos_a"], wl["eos_b"]
-    if wl.get("centre") is not None:
+    if wl.get("centre") is not None and kind != "reference":
+        # the reference's own initialiser always places the droplet at
+        # (DX/2, DY/2, R+2); placement does not change the work per update
         kw["centre"] = (dx / 2, dy / 2, min(wl["centre"][2], dz / 2))
     s = O.Setup(**kw)
     g, l = O.coexistence(model, tr, s.eos_a, s.eos_b)
@@ -422,11 +424,25 @@ def cpu_sample(args, wl: dict) -> dict:
             "kind": kind, "sample": f"{steps} steps of a {dx}x{dy}x{dz} box, same EOS/T/walls, FP64"}
 
 
+def batch_sample_workload(wl: dict) -> dict:
+    """The first box of a batched workload, as a single-box workload (the CPU
+    legs time the reference on one box; MLUPS is per lattice update)."""
+    rng = np.random.default_rng(wl["seed"])
+    L = int(rng.integers(48, 113))
+    model = int(rng.choice([201, 206, 202]))
+    tr = round(float(rng.uniform(0.6, 0.9)) / 0.005) * 0.005
+    base_pt = float(rng.uniform(-0.06, 0.15))
+    return dict(name=wl["name"] + "_box0", dx=L, dy=L, dz=L, model=model, tr=tr, radius=L / 4, width=5.0,
+                wall_mode=1, base_pt=base_pt, k=0.2, ka=0.001, tau=0.8, centre=(L / 2, L / 2, 3.0))
+
+
 def run_reference(args) -> None:
     ws, rank, local = dist_env()
     if rank != 0:
         return
     wl = WORKLOADS[args.workload]
+    if "batch" in wl:
+        wl = batch_sample_workload(wl)
     for _ in range(args.warmup):
         pass
     samples = []
