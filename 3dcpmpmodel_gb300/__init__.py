@@ -165,6 +165,24 @@ class Solver:
             _abi.check(rc)
         return {k: getattr(d, k) for k, _ in Diag._fields_}
 
+    def set_kappa(self, ka: float):
+        _abi.check(self._lib.cpmp_set_kappa(self._h, C.c_double(ka)))
+
+    def adjoint(self, steps: int, target_rho: np.ndarray, checkpoint_every: int = 0):
+        """Loss sum_fluid (rho^T - target)^2 after `steps` steps from the
+        current state, and its gradients w.r.t. the wall field (2*DX*DY) and
+        kappa (sqrt(T) checkpoint-and-recompute).  Returns (loss, grad_wall,
+        grad_kappa); the state is left at step `steps`."""
+        t = np.ascontiguousarray(target_rho, dtype=np.float64).reshape(-1)
+        if t.size != self.n:
+            raise ValueError("target must have N values")
+        gw = np.zeros(2 * self.dx * self.dy, np.float64)
+        loss, gk = C.c_double(), C.c_double()
+        _abi.check(self._lib.cpmp_adjoint(self._h, int(steps), int(checkpoint_every),
+                                          t.ctypes.data_as(C.c_void_p), C.byref(loss),
+                                          gw.ctypes.data_as(C.c_void_p), C.byref(gk)))
+        return loss.value, gw, gk.value
+
     def autotune(self) -> dict:
         """Pick the fused kernel's tile shape and march length by timing them
         on a scratch copy of the current state."""

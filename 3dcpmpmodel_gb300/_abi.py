@@ -83,6 +83,9 @@ SIGNATURES = {
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double), C.c_int]),
     "cpmp_launch_count": (C.c_longlong, [C.c_void_p]),
+    "cpmp_set_kappa": (C.c_int, [C.c_void_p, C.c_double]),
+    "cpmp_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double),
+                               C.c_void_p, C.POINTER(C.c_double)]),
     "cpmp_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "cpmp_batch_handle": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "cpmp_batch_count": (C.c_int, [C.c_void_p]),

@@ -27,6 +27,8 @@ UNITS = [
     ("k_plain_f64.cu", ["--fmad=false"]),
     ("k_fused.cu", []),
     ("k_diag.cu", []),
+    ("k_adjoint_f32.cu", []),
+    ("k_adjoint_f64.cu", ["--fmad=false"]),
 ]
 
 

@@ -1228,3 +1228,144 @@ void cpmp_batch_destroy(cpmp_batch *b)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ adjoint --
+namespace {
+
+// Forward run with sqrt(T) checkpoints, loss, reverse sweep (PLAIN scheme).
+template <class R>
+cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host, double *loss_out,
+                        double *gwall_out, double *gka_out)
+{
+    const size_t n = (size_t)h->n, np = (size_t)h->p.dx * h->p.dy;
+    const size_t state = 23 * n;  // f (19N) | rho (N) | u (3N)
+    const int nck = (T + S - 1) / S;
+    std::vector<void *> mem;
+    auto alloc = [&](void **p, size_t bytes, const char *what) -> cpmp_status {
+        cpmp_status s = dalloc(p, bytes, what);
+        if (s == CPMP_OK) mem.push_back(*p);
+        return s;
+    };
+    auto release = [&]() {
+        for (void *q : mem) cudaFree(q);
+        mem.clear();
+    };
+    R *ck = nullptr, *seg = nullptr, *rr = nullptr, *ur = nullptr, *mur = nullptr, *Fr = nullptr, *mvr = nullptr;
+    double *target = nullptr;
+    AdjBufs<R> b{};
+    const KParams<R> kp = make_kparams<R>(h);
+    const dim3 g3((unsigned)((h->p.dz + 127) / 128), (unsigned)h->p.dy, (unsigned)h->p.dx);
+    const size_t nblocks = (size_t)g3.x * g3.y * g3.z;
+    cpmp_status s;
+#define ALLOC(ptr, bytes, what)                                           \
+    if ((s = alloc((void **)&(ptr), (bytes), (what))) != CPMP_OK) {       \
+        release();                                                        \
+        return s;                                                         \
+    }
+    ALLOC(ck, (size_t)nck * state * sizeof(R), "adjoint checkpoints");
+    ALLOC(seg, (size_t)S * state * sizeof(R), "adjoint segment");
+    ALLOC(rr, n * sizeof(R), "adjoint rho");
+    ALLOC(ur, 3 * n * sizeof(R), "adjoint u");
+    ALLOC(mur, n * sizeof(R), "adjoint mu");
+    ALLOC(Fr, 3 * n * sizeof(R), "adjoint F");
+    ALLOC(mvr, 3 * n * sizeof(R), "adjoint mv");
+    ALLOC(target, n * sizeof(double), "adjoint target");
+    ALLOC(b.lam, 19 * n * sizeof(R), "lambda");
+    ALLOC(b.lam_next, 19 * n * sizeof(R), "lambda");
+    ALLOC(b.lamp, 19 * n * sizeof(R), "lambda partial");
+    ALLOC(b.lamF, 3 * n * sizeof(R), "lambda F");
+    ALLOC(b.lammu, n * sizeof(R), "lambda mu");
+    ALLOC(b.lamrho, n * sizeof(R), "lambda rho");
+    ALLOC(b.ka_part, nblocks * sizeof(double), "kappa partials");
+    ALLOC(b.gka, sizeof(double), "kappa gradient");
+    ALLOC(b.gwall, 2 * np * sizeof(double), "wall gradient");
+    ALLOC(b.loss, sizeof(double), "loss");
+#undef ALLOC
+    cudaStream_t st = h->st;
+    CK(cudaMemcpyAsync(target, target_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(b.gka, 0, sizeof(double), st));
+    CK(cudaMemsetAsync(b.gwall, 0, 2 * np * sizeof(double), st));
+    auto save = [&](R *dst) {
+        cudaMemcpyAsync(dst, h->fb[h->cur], 19 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(dst + 19 * n, h->rho, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(dst + 20 * n, h->u, 3 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+    };
+    // forward, checkpoint every S steps (the handle's own state advances to T)
+    for (int t = 0; t < T; ++t) {
+        if (t % S == 0) save(ck + (size_t)(t / S) * state);
+        launch_one_step(h, nullptr);
+    }
+    adj_launch_loss<R>(kp, h->type, (const R *)h->rho, target, b, st);
+    CK(cudaGetLastError());
+    // reverse sweep, one segment at a time
+    for (int kseg = nck - 1; kseg >= 0; --kseg) {
+        const int n0 = kseg * S, n1 = std::min(n0 + S, T);
+        cudaMemcpyAsync(seg, ck + (size_t)kseg * state, state * sizeof(R), cudaMemcpyDeviceToDevice, st);
+        for (int m = 1; m < n1 - n0; ++m) {  // replay the forward inside the segment
+            R *prev = seg + (size_t)(m - 1) * state, *cur = seg + (size_t)m * state;
+            cudaMemcpyAsync(cur + 19 * n, prev + 19 * n, 4 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+            plain_launch_step<R, R>(kp, h->type, cur + 19 * n, mur, cur + 20 * n, Fr, mvr, prev, cur, st, nullptr);
+        }
+        for (int t = n1 - 1; t >= n0; --t) {
+            const R *stt = seg + (size_t)(t - n0) * state;
+            cudaMemcpyAsync(rr, stt + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(ur, stt + 20 * n, 3 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+            plain_launch_mu_force<R>(kp, h->type, rr, mur, Fr, st);  // walls, mu, F of step t
+            adj_launch_step<R>(kp, h->type, stt, rr, ur, mur, Fr, b, st);
+            std::swap(b.lam, b.lam_next);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            release();
+            return fail(CPMP_ERR_CUDA, std::string("adjoint sweep: ") + cudaGetErrorString(e));
+        }
+    }
+    std::vector<double> gw(2 * np);
+    double loss = 0, gka = 0;
+    cudaMemcpyAsync(&loss, b.loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&gka, b.gka, sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(gw.data(), b.gwall, 2 * np * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    release();
+    if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("adjoint: ") + cudaGetErrorString(e));
+    h->launches += (long long)T * h->launches_per_step * 2 + (long long)T * 12;
+    if (loss_out) *loss_out = loss;
+    if (gka_out) *gka_out = gka;
+    if (gwall_out) std::memcpy(gwall_out, gw.data(), 2 * np * sizeof(double));
+    return CPMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cpmp_status cpmp_set_kappa(cpmp_handle *h, double ka)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    h->p.ka = ka;
+    if (h->gexec) {  // captured launches carry the parameters by value
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_adjoint(cpmp_handle *h, int steps, int checkpoint_every, const double *target_rho,
+                         double *loss, double *grad_wall, double *grad_kappa)
+{
+    if (!h || !target_rho) return fail(CPMP_ERR_PARAM, "null argument");
+    if (!h->plain) return fail(CPMP_ERR_UNSUPPORTED, "the adjoint runs on the PLAIN scheme");
+    if (h->p.k1 != 0.0 || h->p.k2 != 0.0)
+        return fail(CPMP_ERR_UNSUPPORTED, "the K1/K2 pressure-tensor term is not differentiated");
+    if (!h->initialised) return fail(CPMP_ERR_PARAM, "initialise the state first");
+    if (steps < 1) return fail(CPMP_ERR_PARAM, "steps must be >= 1");
+    int S = checkpoint_every;
+    if (S <= 0) S = (int)std::ceil(std::sqrt((double)steps));
+    S = std::max(1, std::min(S, steps));
+    CK(cudaSetDevice(h->p.device));
+    CK(cudaStreamSynchronize(h->st));
+    if (h->f64) return adjoint_run<double>(h, steps, S, target_rho, loss, grad_wall, grad_kappa);
+    return adjoint_run<float>(h, steps, S, target_rho, loss, grad_wall, grad_kappa);
+}
+
+}  // extern "C"

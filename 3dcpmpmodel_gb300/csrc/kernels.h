@@ -81,6 +81,23 @@ void fused_launch_encode(int storage, const KParams<float> &p, int P, void *h, f
 void fused_launch_velocity(int storage, const KParams<float> &p, int P, const void *h,
                            const float *f0, const float *rho, float *u, cudaStream_t st);
 
+// ---- adjoint (k_adjoint_f32.cu, k_adjoint_f64.cu) ---------------------------
+template <class R>
+struct AdjBufs {
+    R *lam, *lam_next, *lamp, *lamF, *lammu, *lamrho;
+    double *ka_part, *gka, *gwall, *loss;
+};
+template <class R>
+void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, const double *target, AdjBufs<R> &b,
+                     cudaStream_t st);
+template <class R>
+void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *f, const R *rho, const R *u, const R *mu,
+                     const R *F, AdjBufs<R> &b, cudaStream_t st);
+extern template void adj_launch_loss<float>(const KParams<float> &, const uint8_t *, const float *, const double *, AdjBufs<float> &, cudaStream_t);
+extern template void adj_launch_step<float>(const KParams<float> &, const uint8_t *, const float *, const float *, const float *, const float *, const float *, AdjBufs<float> &, cudaStream_t);
+extern template void adj_launch_loss<double>(const KParams<double> &, const uint8_t *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
+extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
+
 // ---- diagnostics (k_diag.cu) ----------------------------------------------
 // Deterministic FP64 reduction: out[0] = sum rho (fluid), out[1] = max |mv|^2,
 // out[2] = non-finite flag.  `partials` holds 3 * diag_partial_blocks(n)

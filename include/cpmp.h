@@ -215,6 +215,23 @@ int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, d
 /* Number of the library's own kernel launches issued so far by this handle. */
 long long cpmp_launch_count(cpmp_handle *h);
 
+/* ---- Adjoint ---------------------------------------------------------------
+ * No reference counterpart.  Sets kappa (Ka) of a handle (e.g. between
+ * gradient evaluations); the next step uses it. */
+cpmp_status cpmp_set_kappa(cpmp_handle *h, double ka);
+
+/* Gradient of J = sum over fluid nodes of (rho^T - target)^2, rho^T the
+ * density after `steps` steps from the handle's current state, with respect
+ * to the wall chemical potential (2*DX*DY values, layout of
+ * cpmp_set_wall_field) and kappa.  PLAIN scheme (FP32 or FP64), K1 = K2 = 0.
+ * Runs the forward with a checkpoint of (f, rho, u) every checkpoint_every
+ * steps (<= 0: ceil(sqrt(steps))), then the reverse sweep segment by segment,
+ * replaying each segment's forward from its checkpoint.  The handle's state
+ * is left at step `steps`.  target_rho: N host doubles; grad_wall: 2*DX*DY
+ * host doubles (may be NULL); loss, grad_kappa: host scalars (may be NULL). */
+cpmp_status cpmp_adjoint(cpmp_handle *h, int steps, int checkpoint_every, const double *target_rho,
+                         double *loss, double *grad_wall, double *grad_kappa);
+
 /* ---- Batches: many independent boxes stepped by one persistent launch ----
  * No reference counterpart (the reference runs one box per process).  All
  * boxes use the FUSED scheme and share storage, lap_order, wall_mode,
