@@ -97,6 +97,6 @@ def test_autograd_function(cpmp, problem):
     s = ag._solver(st, w0, 0.01)
     loss, gw, gk = s.adjoint(STEPS, target)
     s.close()
-    assert float(J) == pytest.approx(loss, rel=1e-14)
+    assert float(J.detach()) == pytest.approx(loss, rel=1e-14)
     assert np.allclose(w.grad.numpy(), 2.0 * gw[: 24 * 16].reshape(24, 16), rtol=0, atol=0)
     assert float(k.grad) == pytest.approx(2.0 * gk, rel=1e-14)
