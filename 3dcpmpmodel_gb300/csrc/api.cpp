@@ -1238,7 +1238,8 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
                         double *gwall_out, double *gka_out)
 {
     const size_t n = (size_t)h->n, np = (size_t)h->p.dx * h->p.dy;
-    const size_t state = 23 * n;  // f (19N) | rho (N) | u (3N)
+    const size_t state = 23 * n;    // checkpoint: f (19N) | rho (N) | u (3N)
+    const size_t sstate = 27 * n;   // segment state: f | rho | u | mu (N) | F (3N)
     const int nck = (T + S - 1) / S;
     std::vector<void *> mem;
     auto alloc = [&](void **p, size_t bytes, const char *what) -> cpmp_status {
@@ -1250,7 +1251,7 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
         for (void *q : mem) cudaFree(q);
         mem.clear();
     };
-    R *ck = nullptr, *seg = nullptr, *rr = nullptr, *ur = nullptr, *mur = nullptr, *Fr = nullptr, *mvr = nullptr;
+    R *ck = nullptr, *seg = nullptr, *rr = nullptr, *mur = nullptr, *Fr = nullptr, *mvr = nullptr;
     double *target = nullptr;
     AdjBufs<R> b{};
     const KParams<R> kp = make_kparams<R>(h);
@@ -1263,9 +1264,8 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
         return s;                                                         \
     }
     ALLOC(ck, (size_t)nck * state * sizeof(R), "adjoint checkpoints");
-    ALLOC(seg, (size_t)S * state * sizeof(R), "adjoint segment");
+    ALLOC(seg, (size_t)S * sstate * sizeof(R), "adjoint segment");
     ALLOC(rr, n * sizeof(R), "adjoint rho");
-    ALLOC(ur, 3 * n * sizeof(R), "adjoint u");
     ALLOC(mur, n * sizeof(R), "adjoint mu");
     ALLOC(Fr, 3 * n * sizeof(R), "adjoint F");
     ALLOC(mvr, 3 * n * sizeof(R), "adjoint mv");
@@ -1299,19 +1299,28 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     CK(cudaGetLastError());
     // reverse sweep, one segment at a time
     for (int kseg = nck - 1; kseg >= 0; --kseg) {
-        const int n0 = kseg * S, n1 = std::min(n0 + S, T);
+        const int n0 = kseg * S, n1 = std::min(n0 + S, T), len = n1 - n0;
         cudaMemcpyAsync(seg, ck + (size_t)kseg * state, state * sizeof(R), cudaMemcpyDeviceToDevice, st);
-        for (int m = 1; m < n1 - n0; ++m) {  // replay the forward inside the segment
-            R *prev = seg + (size_t)(m - 1) * state, *cur = seg + (size_t)m * state;
+        // replay the forward inside the segment; the step from state m-1 to m
+        // evaluates mu and F of state m-1 straight into its segment slot
+        for (int m = 1; m < len; ++m) {
+            R *prev = seg + (size_t)(m - 1) * sstate, *cur = seg + (size_t)m * sstate;
             cudaMemcpyAsync(cur + 19 * n, prev + 19 * n, 4 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            plain_launch_step<R, R>(kp, h->type, cur + 19 * n, mur, cur + 20 * n, Fr, mvr, prev, cur, st, nullptr);
+            plain_launch_step<R, R>(kp, h->type, cur + 19 * n, prev + 23 * n, cur + 20 * n, prev + 24 * n, mvr,
+                                    prev, cur, st, nullptr);
+        }
+        {   // the last state of the segment is never stepped from: its mu, F
+            R *last = seg + (size_t)(len - 1) * sstate;
+            cudaMemcpyAsync(rr, last + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
+            plain_launch_mu_force<R>(kp, h->type, rr, last + 23 * n, last + 24 * n, st);
         }
         for (int t = n1 - 1; t >= n0; --t) {
-            const R *stt = seg + (size_t)(t - n0) * state;
+            const R *stt = seg + (size_t)(t - n0) * sstate;
+            // density of step t with its wall layers (the stored copy's solid
+            // layers belong to the step before)
             cudaMemcpyAsync(rr, stt + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            cudaMemcpyAsync(ur, stt + 20 * n, 3 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            plain_launch_mu_force<R>(kp, h->type, rr, mur, Fr, st);  // walls, mu, F of step t
-            adj_launch_step<R>(kp, h->type, stt, rr, ur, mur, Fr, b, st);
+            plain_launch_wall<R>(kp, rr, st);
+            adj_launch_step<R>(kp, h->type, stt, rr, stt + 20 * n, stt + 23 * n, stt + 24 * n, b, st);
             std::swap(b.lam, b.lam_next);
         }
         cudaError_t e = cudaGetLastError();

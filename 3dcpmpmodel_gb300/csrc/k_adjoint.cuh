@@ -200,6 +200,36 @@ __global__ void __launch_bounds__(128) k_adj_force(KParams<R> p, const uint8_t *
     lamrho[I] += add;
 }
 
+// Laplacians of an R field evaluated in FP64 (for the kappa gradient).
+template <class R>
+__device__ __forceinline__ double lap5_d(const KParams<R> &p, const R *x, int i, int j, int k)
+{
+    auto X = [&](int a, int b, int c) -> double { return (double)x[nid(p, a, b, c)]; };
+    const int im2 = wrap_off(i - 2, p.dx), im1 = wrap_off(i - 1, p.dx), ip1 = wrap_off(i + 1, p.dx),
+              ip2 = wrap_off(i + 2, p.dx);
+    const int jm2 = wrap_off(j - 2, p.dy), jm1 = wrap_off(j - 1, p.dy), jp1 = wrap_off(j + 1, p.dy),
+              jp2 = wrap_off(j + 2, p.dy);
+    const int km2 = wrap_off(k - 2, p.dz), km1 = wrap_off(k - 1, p.dz), kp1 = wrap_off(k + 1, p.dz),
+              kp2 = wrap_off(k + 2, p.dz);
+    return (-X(i, j, k) * 90.0 + (-X(im2, j, k) + X(im1, j, k) * 16.0 + X(ip1, j, k) * 16.0 - X(ip2, j, k)) +
+            (-X(i, jm2, k) + X(i, jm1, k) * 16.0 + X(i, jp1, k) * 16.0 - X(i, jp2, k)) +
+            (-X(i, j, km2) + X(i, j, km1) * 16.0 + X(i, j, kp1) * 16.0 - X(i, j, kp2))) /
+           12.0;
+}
+template <class R>
+__device__ __forceinline__ double lap7_d(const KParams<R> &p, const R *x, int i, int j, int k)
+{
+    auto X = [&](int a, int b, int c) -> double { return (double)x[nid(p, a, b, c)]; };
+    double s = -X(i, j, k) * 1470.0;
+#pragma unroll
+    for (int d = 1; d <= 3; ++d) {
+        const double w = d == 1 ? 270.0 : (d == 2 ? -27.0 : 2.0);
+        s += w * (X(wrap_off(i + d, p.dx), j, k) + X(wrap_off(i - d, p.dx), j, k) + X(i, wrap_off(j + d, p.dy), k) +
+                  X(i, wrap_off(j - d, p.dy), k) + X(i, j, wrap_off(k + d, p.dz)) + X(i, j, wrap_off(k - d, p.dz)));
+    }
+    return s / 180.0;
+}
+
 // R4: chemical-potential adjoint; per-block FP64 partials of dJ/dka.
 template <class R>
 __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *type, const R *rho, const R *lammu,
@@ -249,8 +279,10 @@ __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *typ
         if (type[I] == FLUID) {
             const R r = rho[I];
             add += p.kk * dmu0<R>(p.eos, p.A, p.B, p.T, r) * lammu[I];
-            const R lr = p.lap_order == 7 ? lap7sum_g(p, rho, i, j, k) / R(180) : lap5_g(p, rho, i, j, k);
-            gka = -(double)lammu[I] * (double)lr;
+            // the Laplacian of this term in FP64: it is a small difference of
+            // O(rho_l) values summed over every node and step
+            const double lr = p.lap_order == 7 ? lap7_d(p, rho, i, j, k) : lap5_d(p, rho, i, j, k);
+            gka = -(double)lammu[I] * lr;
         }
         lamrho[I] += add;
     }

@@ -335,6 +335,16 @@ void plain_launch_macro(const KParams<R> &p, const uint8_t *type, const S *f, R 
     k_macro<R, S><<<g, 128, 0, st>>>(p, type, f, rho, u);
 }
 
+// Wall layers of rho only (adjoint recompute).
+template <class R>
+void plain_launch_wall(const KParams<R> &p, R *rho, cudaStream_t st)
+{
+    if (p.wall_mode != 1) return;
+    const long long np = (long long)p.dx * p.dy;
+    const unsigned gw = (unsigned)((np + 127) / 128);
+    for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) k_wall_pass<R><<<gw, 128, 0, st>>>(p, s, rho, nullptr);
+}
+
 // mu and F without collision (diagnostic read-back of MU / FORCE).
 template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,

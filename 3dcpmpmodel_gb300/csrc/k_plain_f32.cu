@@ -6,4 +6,5 @@ template void plain_launch_init<float, float>(const KParams<float> &, const Drop
 template void plain_launch_step<float, float>(const KParams<float> &, const uint8_t *, float *, float *, float *, float *, float *, const float *, float *, cudaStream_t, LaunchHook *);
 template void plain_launch_macro<float, float>(const KParams<float> &, const uint8_t *, const float *, float *, float *, cudaStream_t);
 template void plain_launch_mu_force<float>(const KParams<float> &, const uint8_t *, float *, float *, float *, cudaStream_t);
+template void plain_launch_wall<float>(const KParams<float> &, float *, cudaStream_t);
 }  // namespace cpmp

@@ -26,6 +26,10 @@ template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
                            cudaStream_t st);
 
+template <class R>
+void plain_launch_wall(const KParams<R> &p, R *rho, cudaStream_t st);
+extern template void plain_launch_wall<float>(const KParams<float> &, float *, cudaStream_t);
+extern template void plain_launch_wall<double>(const KParams<double> &, double *, cudaStream_t);
 extern template void plain_launch_init<float, float>(const KParams<float> &, const DropletDev &, uint8_t *, float *, float *, float *, float *, cudaStream_t);
 extern template void plain_launch_step<float, float>(const KParams<float> &, const uint8_t *, float *, float *, float *, float *, float *, const float *, float *, cudaStream_t, LaunchHook *);
 extern template void plain_launch_macro<float, float>(const KParams<float> &, const uint8_t *, const float *, float *, float *, cudaStream_t);
