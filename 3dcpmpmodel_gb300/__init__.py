@@ -54,6 +54,29 @@ def default_params(**kw) -> Params:
     return p
 
 
+def tecplot_write(path: str, title: str, zone: str, variables: dict, shape):
+    """Write one ordered zone: variables = {name: numpy array (float32,
+    float64, int32, int16 or int8), I fastest}; shape = (imax, jmax, kmax)."""
+    codes = {np.dtype(np.float32): 1, np.dtype(np.float64): 2, np.dtype(np.int32): 3,
+             np.dtype(np.int16): 4, np.dtype(np.int8): 5}
+    arrs = [np.ascontiguousarray(v) for v in variables.values()]
+    nv = len(arrs)
+    names = (C.c_char_p * nv)(*[k.encode() for k in variables])
+    types = (C.c_int * nv)(*[codes[a.dtype] for a in arrs])
+    ptrs = (C.c_void_p * nv)(*[a.ctypes.data for a in arrs])
+    _abi.check(lib().cpmp_tecplot_write(path.encode(), title.encode(), zone.encode(), nv, names, types, ptrs,
+                                        int(shape[0]), int(shape[1]), int(shape[2])))
+
+
+def dim_velocity(radius: float, diameter: float, tau: float) -> float:
+    """DimV of the reference's DimConversion(Radius*2, Diameter, 7.2, 1.0,
+    Viscosity, 0.01) (FluidCuda.cu:137-139, 474-486), same operation order."""
+    visc = (tau * 2 - 1) / 6
+    dim_len = diameter / (radius * 2)
+    dim_time = visc / 0.01 * (dim_len * dim_len)
+    return dim_len / dim_time
+
+
 def coexistence(model: int, tr: float, eos_a=0.0, eos_b=0.0, eos_omega=0.0, cocurve_dir=None):
     """SetMultiphase stand-alone: dict of den_g, den_l, A, B, Tc, Rc."""
     out = [C.c_double() for _ in range(6)]
@@ -164,6 +187,14 @@ class Solver:
         if rc != 0 and not (allow_nonfinite and rc == _abi.CPMP_ERR_NONFINITE):
             _abi.check(rc)
         return {k: getattr(d, k) for k, _ in Diag._fields_}
+
+    def write_tecplot(self, path: str, layout: str = "savetask", decimate: int = 5,
+                      reference_stride: bool = False, vel_scale: float = 1.0):
+        """Tecplot binary output in the reference's SaveTask / SaveAllByType
+        layouts; vel_scale is the reference's DimV (see dim_velocity)."""
+        lay = {"savetask": 0, "allbytype": 1}[layout]
+        _abi.check(self._lib.cpmp_write_tecplot(self._h, path.encode(), lay, int(decimate),
+                                                1 if reference_stride else 0, float(vel_scale)))
 
     def set_kappa(self, ka: float):
         _abi.check(self._lib.cpmp_set_kappa(self._h, C.c_double(ka)))

@@ -83,6 +83,10 @@ SIGNATURES = {
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
                                     C.POINTER(C.c_double), C.c_int]),
     "cpmp_launch_count": (C.c_longlong, [C.c_void_p]),
+    "cpmp_tecplot_write": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "cpmp_write_tecplot": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "cpmp_get_dims": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "cpmp_set_kappa": (C.c_int, [C.c_void_p, C.c_double]),
     "cpmp_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double),
                                C.c_void_p, C.POINTER(C.c_double)]),

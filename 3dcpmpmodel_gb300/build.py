@@ -23,6 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE
 UNITS = [
     ("api.cpp", []),
     ("eos.cpp", []),
+    ("tecplot.cpp", []),
     ("k_plain_f32.cu", []),
     ("k_plain_f64.cu", ["--fmad=false"]),
     ("k_fused.cu", []),

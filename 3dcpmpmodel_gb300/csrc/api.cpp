@@ -1348,6 +1348,15 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
 
 extern "C" {
 
+cpmp_status cpmp_get_dims(cpmp_handle *h, int *dims)
+{
+    if (!h || !dims) return fail(CPMP_ERR_PARAM, "null argument");
+    dims[0] = h->p.dx;
+    dims[1] = h->p.dy;
+    dims[2] = h->p.dz;
+    return CPMP_OK;
+}
+
 cpmp_status cpmp_set_kappa(cpmp_handle *h, double ka)
 {
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");

@@ -215,6 +215,37 @@ int cpmp_kernel_times(cpmp_handle *h, const char **names, long long *launches, d
 /* Number of the library's own kernel launches issued so far by this handle. */
 long long cpmp_launch_count(cpmp_handle *h);
 
+/* ---- Tecplot output --------------------------------------------------------
+ * The reference's on-disk output format: Tecplot binary "#!TDV112", one
+ * ordered zone (ordered_tec.cpp:674-717, 990-1147). */
+enum { CPMP_TEC_FLOAT = 1, CPMP_TEC_DOUBLE = 2, CPMP_TEC_INT32 = 3, CPMP_TEC_INT16 = 4, CPMP_TEC_BYTE = 5 };
+/* Layouts of cpmp_write_tecplot: SaveTask (FluidCuda.cu:901-927): variables
+ * i, j, k (int16) and Density (double) on the grid decimated by `decimate`,
+ * I = z fastest; SaveAllByType (FluidCuda.cu:1032-1092): i, j, k, Ux, Uy, Uz
+ * (physical velocity where rho >= (rho_g + rho_l)/2, else -2) and Density,
+ * all double, x fastest. */
+enum { CPMP_TEC_SAVETASK = 0, CPMP_TEC_ALLBYTYPE = 1 };
+/* flags: sample the density like the reference's CompressField, which
+ * strides the flat node index instead of each axis (FluidCuda.cu:470). */
+enum { CPMP_TEC_REFERENCE_STRIDE = 1 };
+
+/* Writes one ordered zone of nvar variables (types CPMP_TEC_*, each
+ * imax*jmax*kmax values, I fastest) to `path`.  Host only; needs no GPU. */
+cpmp_status cpmp_tecplot_write(const char *path, const char *title, const char *zone_name, int nvar,
+                               const char *const *names, const int *types, const void *const *data,
+                               int imax, int jmax, int kmax);
+/* Writes the handle's current fields in one of the reference's layouts; the
+ * zone is named after the file (path without directory and ".plt").  A
+ * decimated extent of 0 (DY < decimate) is written as 1, where the reference
+ * writer throws.  vel_scale multiplies the ALLBYTYPE velocities: the
+ * reference's DimV = DimLen / DimTime from DimConversion (FluidCuda.cu:474-486;
+ * 1 keeps lattice units, and the reference's default Diameter = 0 makes it
+ * NaN). */
+cpmp_status cpmp_write_tecplot(cpmp_handle *h, const char *path, int layout, int decimate, int flags,
+                               double vel_scale);
+/* Grid dimensions of a handle: dims[3] = DX, DY, DZ. */
+cpmp_status cpmp_get_dims(cpmp_handle *h, int *dims);
+
 /* ---- Adjoint ---------------------------------------------------------------
  * No reference counterpart.  Sets kappa (Ka) of a handle (e.g. between
  * gradient evaluations); the next step uses it. */

@@ -68,6 +68,19 @@ def compile_lib() -> str:
     return out
 
 
+def build_tecplot(src: str = DEFAULT_SRC) -> str | None:
+    """The reference's Tecplot writer (ordered_tec.cpp, compiled from the
+    reference tree where it lies) behind oracle/tec_ref_driver.cpp."""
+    if not os.path.isfile(os.path.join(src, "ordered_tec.cpp")):
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    out = os.path.join(OUT, "libtecref.so")
+    subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-w", "-std=c++17", "-I", src,
+                    os.path.join(HERE, "tec_ref_driver.cpp"), os.path.join(src, "ordered_tec.cpp"), "-o", out],
+                   check=True)
+    return out
+
+
 def build(src: str = DEFAULT_SRC) -> str | None:
     """Generate (when the reference tree exists) and compile; returns the .so
     path, or None when neither the reference tree nor generated files exist."""
@@ -84,5 +97,6 @@ if __name__ == "__main__":
     ap.add_argument("--src", default=DEFAULT_SRC)
     a = ap.parse_args()
     p = build(a.src)
-    print(p if p else "reference sources unavailable; nothing built")
+    t = build_tecplot(a.src)
+    print(p if p else "reference sources unavailable; nothing built", t or "")
     sys.exit(0)
