@@ -16,10 +16,12 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcpmp.so")
+RUNNER = os.path.join(HERE, "cpmp_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
 # (source, extra flags)
+# the library's units; cpmp_run.cpp is the separate driver executable
 UNITS = [
     ("api.cpp", []),
     ("eos.cpp", []),
@@ -57,9 +59,26 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
+def build_runner() -> str:
+    """The cpmp_run command-line driver, linked against libcpmp.so with an
+    $ORIGIN run path (host code only)."""
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(CSRC, "cpmp_run.cpp"),
+           "-L", HERE, "-lcpmp", "-Wl,-rpath,$ORIGIN", "-o", RUNNER + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cpmp_run failed to build:\n{r.stdout}\n{r.stderr}")
+    os.replace(RUNNER + ".tmp", RUNNER)
+    return RUNNER
+
+
 def build(force: bool = False, jobs: int | None = None) -> str:
-    """Compile and link libcpmp.so unless it is newer than every source."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+    """Compile and link libcpmp.so (and the cpmp_run driver) unless they are
+    newer than every source."""
+    fresh = lambda f: os.path.exists(f) and os.path.getmtime(f) >= _sources_mtime()  # noqa: E731
+    if not force and fresh(LIB) and fresh(RUNNER):
+        return LIB
+    if not force and fresh(LIB):
+        build_runner()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     jobs = jobs or min(len(UNITS), os.cpu_count() or 4)
@@ -71,6 +90,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_runner()
     return LIB
 
 

@@ -1270,12 +1270,12 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     ALLOC(Fr, 3 * n * sizeof(R), "adjoint F");
     ALLOC(mvr, 3 * n * sizeof(R), "adjoint mv");
     ALLOC(target, n * sizeof(double), "adjoint target");
-    ALLOC(b.lam, 19 * n * sizeof(R), "lambda");
-    ALLOC(b.lam_next, 19 * n * sizeof(R), "lambda");
     ALLOC(b.lamp, 19 * n * sizeof(R), "lambda partial");
+    ALLOC(b.lamp_next, 19 * n * sizeof(R), "lambda partial");
     ALLOC(b.lamF, 3 * n * sizeof(R), "lambda F");
     ALLOC(b.lammu, n * sizeof(R), "lambda mu");
     ALLOC(b.lamrho, n * sizeof(R), "lambda rho");
+    ALLOC(b.lamrho_next, n * sizeof(R), "lambda rho");
     ALLOC(b.ka_part, nblocks * sizeof(double), "kappa partials");
     ALLOC(b.gka, sizeof(double), "kappa gradient");
     ALLOC(b.gwall, 2 * np * sizeof(double), "wall gradient");
@@ -1320,8 +1320,9 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
             // layers belong to the step before)
             cudaMemcpyAsync(rr, stt + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
             plain_launch_wall<R>(kp, rr, st);
-            adj_launch_step<R>(kp, h->type, stt, rr, stt + 20 * n, stt + 23 * n, stt + 24 * n, b, st);
-            std::swap(b.lam, b.lam_next);
+            adj_launch_step<R>(kp, h->type, rr, stt + 20 * n, stt + 23 * n, stt + 24 * n, b, st);
+            std::swap(b.lamp, b.lamp_next);
+            std::swap(b.lamrho, b.lamrho_next);
         }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {

@@ -7,11 +7,13 @@
 //   F        = -rho G(mu) + G(rho)/3                (NonidealForce)
 //   f*       = M^-1 [ (I-S) M f + S meq(rho,u) + meq(rho, u+F/rho) - meq(rho,u) ]
 //   f^{n+1}  = stream(f*) with half-way bounce-back (GlobalCollide)
-// Given lam = dJ/df^{n+1} the reverse step produces dJ/df^n and accumulates
+// dJ/df^n is kept in factored form: lamp_q(x) + lamrho(x) on fluid nodes
+// (0 on solid ones), so the sum is never written out.  Given that pair for
+// step n+1 the reverse step produces the pair of step n and accumulates
 // dJ/dw (wall field) and dJ/dka:
-//   R2  k_adj_collide : pull lam through the streaming (bounce-back
-//       transposed), collision adjoint in moment space -> partial dJ/df,
-//       dJ/dF, the collision's dJ/drho
+//   R2  k_adj_collide : pull dJ/df^{n+1} = lamp + lamrho through the streaming
+//       (bounce-back transposed), collision adjoint in moment space ->
+//       lamp (partial dJ/df), dJ/dF, the collision's dJ/drho
 //   R3  k_adj_force   : dJ/dmu(y) = sum_a G_a(rho lamF_a)(y),
 //       dJ/drho(y) += -sum_a G_a(lamF_a)(y)/3 - lamF(y).G(mu)(y)
 //       (the gradient stencils are antisymmetric, so their transpose is the
@@ -20,10 +22,12 @@
 //       fluid)(y) (the Laplacian is symmetric); dJ/dka += -sum lam_mu Lap(rho)
 //   R5  k_adj_wall    : wall layers back onto the first fluid layer (the
 //       6-point average is symmetric), dJ/dw += lam_mu on the solid layers
-//   R6  k_adj_finish  : dJ/df^n_q(x) = partial_q(x) + dJ/drho(x)
+//   (R6, dJ/df^n_q = lamp_q + lamrho, is folded into the next R2's gather)
 // The K1/K2 pressure-tensor term is not differentiated (callers get
 // CPMP_ERR_UNSUPPORTED when it is active).
 #pragma once
+
+#include <type_traits>
 
 #include "k_plain.cuh"
 #include "kernels.h"
@@ -83,9 +87,9 @@ __device__ __forceinline__ void meq_adjoint(R rho, R vx, R vy, R vz, const R Aw[
 
 // R2: collision + streaming adjoint (one thread per node, 3-D grid).
 template <class R>
-__global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t *type, const R *f,
-                                                     const R *rho, const R *u, const R *F, const R *lam_next,
-                                                     R *lamp, R *lamF, R *lamrho)
+__global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t *type, const R *rho,
+                                                     const R *u, const R *F, const R *lamp_next,
+                                                     const R *lamrho_next, R *lamp, R *lamF, R *lamrho)
 {
     NODE3D(p);
     const long long n = p.n;
@@ -100,11 +104,12 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     // push streaming; a population bounced back at a solid destination came
     // back into slot opp(q) of this node
     R ls[Q];
+    const R lr_here = lamrho_next[I];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int ii = wrap_off(i + cx(q), p.dx), jj = wrap_off(j + cy(q), p.dy), kk = wrap_off(k + cz(q), p.dz);
         const long long D = nid(p, ii, jj, kk);
-        ls[q] = type[D] == FLUID ? lam_next[q * n + D] : lam_next[opp(q) * n + I];
+        ls[q] = type[D] == FLUID ? lamp_next[q * n + D] + lamrho_next[D] : lamp_next[opp(q) * n + I] + lr_here;
     }
     // mu* = M^-T lambda* = diag(1/norm) M lambda*
     R ms[Q];
@@ -166,30 +171,43 @@ __global__ void __launch_bounds__(128) k_adj_force(KParams<R> p, const uint8_t *
         b[d + 3] = wrap_off(j + d, p.dy);
         c[d + 3] = wrap_off(k + d, p.dz);
     }
-    // psi_a = rho * lamF_a and lamF_a (both zero on solid nodes: lamF is)
+    // for each lattice line (sx, sy, sz) with weight vector w (2 e on the
+    // axes, e on the diagonals): sum_d c_d (v(+d) - v(-d)) of v = w . lamF
+    // and of rho v; only the nonzero components of w are loaded
     R gm = R(0), gr = R(0);
-    // for each lattice line and component weight: sum_d c_d (v(+d) - v(-d))
-    auto acc = [&](int sx, int sy, int sz, R wx, R wy, R wz) {
+    auto acc = [&](auto SX, auto SY, auto SZ) {
+        constexpr int sx = decltype(SX)::value, sy = decltype(SY)::value, sz = decltype(SZ)::value;
+        constexpr int axis = (sx != 0) + (sy != 0) + (sz != 0) == 1;
+        constexpr int wx = axis ? 2 * sx : sx, wy = axis ? 2 * sy : sy, wz = axis ? 2 * sz : sz;
+        auto lw = [&](long long P) -> R {
+            R v = R(0);
+            if constexpr (wx != 0) v += R(wx) * lamF[P];
+            if constexpr (wy != 0) v += R(wy) * lamF[P + n];
+            if constexpr (wz != 0) v += R(wz) * lamF[P + 2 * n];
+            return v;
+        };
 #pragma unroll
         for (int d = 1; d <= 3; ++d) {
             const R cd = d == 1 ? R(45) : (d == 2 ? R(-9) : R(1));
             const long long P_ = nid(p, a[3 + sx * d], b[3 + sy * d], c[3 + sz * d]);
             const long long M_ = nid(p, a[3 - sx * d], b[3 - sy * d], c[3 - sz * d]);
-            const R lp = wx * lamF[P_] + wy * lamF[P_ + n] + wz * lamF[P_ + 2 * n];
-            const R lm = wx * lamF[M_] + wy * lamF[M_ + n] + wz * lamF[M_ + 2 * n];
+            const R lp = lw(P_), lm = lw(M_);
             gm += cd * (rho[P_] * lp - rho[M_] * lm);
             gr += cd * (lp - lm);
         }
     };
-    acc(1, 0, 0, R(2), R(0), R(0));
-    acc(0, 1, 0, R(0), R(2), R(0));
-    acc(0, 0, 1, R(0), R(0), R(2));
-    acc(1, 1, 0, R(1), R(1), R(0));
-    acc(1, -1, 0, R(1), R(-1), R(0));
-    acc(1, 0, 1, R(1), R(0), R(1));
-    acc(1, 0, -1, R(1), R(0), R(-1));
-    acc(0, 1, 1, R(0), R(1), R(1));
-    acc(0, 1, -1, R(0), R(1), R(-1));
+    using P1 = std::integral_constant<int, 1>;
+    using Z0 = std::integral_constant<int, 0>;
+    using M1 = std::integral_constant<int, -1>;
+    acc(P1{}, Z0{}, Z0{});
+    acc(Z0{}, P1{}, Z0{});
+    acc(Z0{}, Z0{}, P1{});
+    acc(P1{}, P1{}, Z0{});
+    acc(P1{}, M1{}, Z0{});
+    acc(P1{}, Z0{}, P1{});
+    acc(P1{}, Z0{}, M1{});
+    acc(Z0{}, P1{}, P1{});
+    acc(Z0{}, P1{}, M1{});
     lammu[I] = gm / R(360);
     R add = -gr / R(360) / R(3);
     if (type[I] == FLUID) {
@@ -334,24 +352,12 @@ __global__ void k_adj_wall(KParams<R> p, int pass, const R *lammu, R *lamrho, do
     }
 }
 
-// R6: dJ/df^n = partial + dJ/drho on fluid nodes, 0 on solid nodes.
-template <class R>
-__global__ void __launch_bounds__(128) k_adj_finish(KParams<R> p, const uint8_t *type, const R *lamp,
-                                                    const R *lamrho, R *lam)
-{
-    NODE3D(p);
-    const long long n = p.n;
-    const bool fl = type[I] == FLUID;
-    const R lr = fl ? lamrho[I] : R(0);
-#pragma unroll
-    for (int q = 0; q < Q; ++q) lam[q * n + I] = fl ? lamp[q * n + I] + lr : R(0);
-}
-
 // Loss J = sum over fluid nodes of (rho - target)^2 (FP64 partials) and the
-// terminal adjoint dJ/df^T_q = 2 (rho - target) for every q.
+// terminal adjoint dJ/df^T_q = 2 (rho - target) for every q, in factored
+// form: lamp = 0, lamrho = 2 (rho - target).
 template <class R>
 __global__ void __launch_bounds__(128) k_adj_loss(KParams<R> p, const uint8_t *type, const R *rho,
-                                                  const double *target, R *lam, double *part)
+                                                  const double *target, R *lamp, R *lamrho, double *part)
 {
     __shared__ double red[128];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,7 +372,8 @@ __global__ void __launch_bounds__(128) k_adj_loss(KParams<R> p, const uint8_t *t
             g = (R)(2.0 * d);
         }
 #pragma unroll
-        for (int q = 0; q < Q; ++q) lam[q * p.n + I] = g;
+        for (int q = 0; q < Q; ++q) lamp[q * p.n + I] = R(0);
+        lamrho[I] = g;
     }
     red[threadIdx.x] = l;
     __syncthreads();
@@ -399,19 +406,20 @@ void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, con
                      cudaStream_t st)
 {
     const dim3 g = grid3(p, 128);
-    k_adj_loss<R><<<g, 128, 0, st>>>(p, type, rho, target, b.lam_next, b.ka_part);
+    k_adj_loss<R><<<g, 128, 0, st>>>(p, type, rho, target, b.lamp_next, b.lamrho_next, b.ka_part);
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.loss, 0);
 }
 
 // One reverse step.  rho/u/mu/F hold the forward intermediates of step n
-// (recomputed from f^n by the caller); b.lam_next = dJ/df^{n+1} on entry,
-// b.lam = dJ/df^n on exit.
+// (recomputed from f^n by the caller); (b.lamp_next, b.lamrho_next) =
+// dJ/df^{n+1} on entry, (b.lamp, b.lamrho) = dJ/df^n on exit.
 template <class R>
-void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *f, const R *rho, const R *u, const R *mu,
-                     const R *F, AdjBufs<R> &b, cudaStream_t st)
+void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *mu, const R *F,
+                     AdjBufs<R> &b, cudaStream_t st)
 {
     const dim3 g = grid3(p, 128);
-    k_adj_collide<R><<<g, 128, 0, st>>>(p, type, f, rho, u, F, b.lam_next, b.lamp, b.lamF, b.lamrho);
+    k_adj_collide<R><<<g, 128, 0, st>>>(p, type, rho, u, F, b.lamp_next, b.lamrho_next, b.lamp, b.lamF,
+                                        b.lamrho);
     k_adj_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, b.lamF, b.lammu, b.lamrho);
     k_adj_mu<R><<<g, 128, 0, st>>>(p, type, rho, b.lammu, b.lamrho, b.ka_part);
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.gka, 1);
@@ -420,7 +428,6 @@ void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *f, const
         const unsigned gw = (unsigned)((np + 127) / 128);
         for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) k_adj_wall<R><<<gw, 128, 0, st>>>(p, s, b.lammu, b.lamrho, b.gwall);
     }
-    k_adj_finish<R><<<g, 128, 0, st>>>(p, type, b.lamp, b.lamrho, b.lam);
 }
 
 }  // namespace cpmp

@@ -88,19 +88,21 @@ void fused_launch_velocity(int storage, const KParams<float> &p, int P, const vo
 // ---- adjoint (k_adjoint_f32.cu, k_adjoint_f64.cu) ---------------------------
 template <class R>
 struct AdjBufs {
-    R *lam, *lam_next, *lamp, *lamF, *lammu, *lamrho;
+    // dJ/df^n_q(x) = lamp_q(x) + lamrho(x) on fluid nodes, 0 on solid ones;
+    // the *_next pair holds step n+1 while step n is being formed
+    R *lamp, *lamp_next, *lamrho, *lamrho_next, *lamF, *lammu;
     double *ka_part, *gka, *gwall, *loss;
 };
 template <class R>
 void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, const double *target, AdjBufs<R> &b,
                      cudaStream_t st);
 template <class R>
-void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *f, const R *rho, const R *u, const R *mu,
-                     const R *F, AdjBufs<R> &b, cudaStream_t st);
+void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *mu, const R *F,
+                     AdjBufs<R> &b, cudaStream_t st);
 extern template void adj_launch_loss<float>(const KParams<float> &, const uint8_t *, const float *, const double *, AdjBufs<float> &, cudaStream_t);
-extern template void adj_launch_step<float>(const KParams<float> &, const uint8_t *, const float *, const float *, const float *, const float *, const float *, AdjBufs<float> &, cudaStream_t);
+extern template void adj_launch_step<float>(const KParams<float> &, const uint8_t *, const float *, const float *, const float *, const float *, AdjBufs<float> &, cudaStream_t);
 extern template void adj_launch_loss<double>(const KParams<double> &, const uint8_t *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
-extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
+extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
 
 // ---- diagnostics (k_diag.cu) ----------------------------------------------
 // Deterministic FP64 reduction: out[0] = sum rho (fluid), out[1] = max |mv|^2,
