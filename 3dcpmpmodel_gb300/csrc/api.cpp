@@ -189,8 +189,8 @@ void launch_one_step(cpmp_handle *h, LaunchHook *hook)
         const int P = (int)(h->step & 1);
         fused_launch_wall(k, (float *)h->rho, (float *)h->rho2, h->st, hook);
         fused_launch_collide(h->p.storage, k, P, h->tile, h->h, h->f0[P], h->f0[1 - P], (const float *)h->rho,
-                             (float *)h->rho2, h->st, hook);
-        fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho2, &h->tile, h->st, hook);
+                             h->st, hook);
+        fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho2, h->st, hook);
         std::swap(h->rho, h->rho2);
     }
     h->step += 1;
@@ -372,6 +372,8 @@ cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
     if (p.lap_order != 5 && p.lap_order != 7) return fail(CPMP_ERR_PARAM, "lap_order must be 5 or 7");
     if (p.scheme == CPMP_SCHEME_PLAIN && p.storage != CPMP_STORE_F32 && p.storage != CPMP_STORE_F64)
         return fail(CPMP_ERR_UNSUPPORTED, "PLAIN scheme stores FP32 or FP64 populations");
+    if (p.scheme == CPMP_SCHEME_FUSED && (long long)p.dx * p.dy * p.dz >= (1LL << 32))
+        return fail(CPMP_ERR_UNSUPPORTED, "the FUSED scheme indexes nodes with 32 bits: N must be below 2^32");
     if (p.scheme == CPMP_SCHEME_FUSED && p.storage == CPMP_STORE_F64)
         return fail(CPMP_ERR_UNSUPPORTED, "FUSED scheme stores FP32, FP16 or BF16 populations");
     if (p.scheme != CPMP_SCHEME_PLAIN && p.scheme != CPMP_SCHEME_FUSED) return fail(CPMP_ERR_PARAM, "scheme");
@@ -652,7 +654,7 @@ cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *
         auto k = make_kparams<float>(h);
         if (e == cudaSuccess) {
             fused_launch_encode(h->p.storage, k, P, h->h, h->f0[P], tmp, dtype == CPMP_F64, h->st);
-            fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, nullptr, h->st, nullptr);
+            fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, h->st, nullptr);
             h->launches += 3;
             e = cudaStreamSynchronize(h->st);
         }
@@ -737,12 +739,12 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     const size_t n = (size_t)h->n;
     const size_t hs = h->p.storage == CPMP_STORE_F32 ? 4 : 2;
     // scratch copy of the state: the in-place A-A kernel would otherwise advance it
-    void *sh = nullptr, *sf0a = nullptr, *sf0b = nullptr, *srho = nullptr, *srho2 = nullptr;
+    void *sh = nullptr, *sf0a = nullptr, *sf0b = nullptr, *srho = nullptr;
     cpmp_status s;
     if ((s = dalloc(&sh, (CPMP_Q - 1) * n * hs, "tune h")) != CPMP_OK) return s;
     if ((s = dalloc(&sf0a, n * 4, "tune f0")) != CPMP_OK || (s = dalloc(&sf0b, n * 4, "tune f0")) != CPMP_OK ||
-        (s = dalloc(&srho, n * 4, "tune rho")) != CPMP_OK || (s = dalloc(&srho2, n * 4, "tune rho")) != CPMP_OK) {
-        cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(srho2);
+        (s = dalloc(&srho, n * 4, "tune rho")) != CPMP_OK) {
+        cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho);
         return s;
     }
     const int P0 = (int)(h->step & 1);
@@ -766,17 +768,17 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
             ft.xl = std::min(ft.xl, h->p.dx);
             // warm-up, then time two launches (one of each parity)
             fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
-                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+                                 (const float *)srho, h->st, nullptr);
             cudaEventRecord(e0, h->st);
             fused_launch_collide(h->p.storage, k, 1, ft, sh, (const float *)sf0b, (float *)sf0a,
-                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+                                 (const float *)srho, h->st, nullptr);
             fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
-                                 (const float *)srho, (float *)srho2, h->st, nullptr);
+                                 (const float *)srho, h->st, nullptr);
             cudaEventRecord(e1, h->st);
             cudaError_t e = cudaEventSynchronize(e1);
             if (e != cudaSuccess) {
                 cudaEventDestroy(e0); cudaEventDestroy(e1);
-                cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(srho2);
+                cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho);
                 return fail(CPMP_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
             }
             float ms = 0;
@@ -794,7 +796,6 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     cudaFree(sf0a);
     cudaFree(sf0b);
     cudaFree(srho);
-    cudaFree(srho2);
     CK(cudaGetLastError());
     if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl) {
         h->tile = best;

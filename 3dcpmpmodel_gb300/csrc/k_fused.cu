@@ -126,22 +126,22 @@ void with_storage(int storage, F &&f)
 
 template <class S, int TY, int TZ, int L>
 void launch_collide_t(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
-                      float *f0n, const float *rho, float *rho_next, cudaStream_t st)
+                      float *f0n, const float *rho, cudaStream_t st)
 {
     const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + t.xl - 1) / t.xl);
     k_fused_collide<S, TY, TZ, L><<<grid, TY * TZ, fused_smem_bytes<S, TY, TZ, L>(), st>>>(
-        p, P, h, f0c, f0n, rho, rho_next, t.xl);
+        p, P, h, f0c, f0n, rho, t.xl);
 }
 
 template <class S, int L>
 void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, const float *f0c,
-                      float *f0n, const float *rho, float *rho_next, cudaStream_t st)
+                      float *f0n, const float *rho, cudaStream_t st)
 {
-    if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
-    else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
-    else if (t.ty == 16 && t.tz == 32) launch_collide_t<S, 16, 32, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
-    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
-    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, rho_next, st);
+    if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 16 && t.tz == 32) launch_collide_t<S, 16, 32, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, st);
+    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, st);
 }
 
 // usable[storage index][L - 2][tile index]: the instantiation's shared
@@ -233,30 +233,28 @@ void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, c
 }
 
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, float *rho_next, cudaStream_t st,
+                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
                           LaunchHook *hook)
 {
     hook_begin(hook, K_FUSED, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
         if (p.lap_order == 7)
-            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, rho_next, st);
+            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, st);
         else
-            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, rho_next, st);
+            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, st);
     });
     hook_end(hook, K_FUSED, st);
 }
 
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
-                          const float *f0, float *rho, const FusedTile *fold, cudaStream_t st, LaunchHook *hook)
+                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook)
 {
-    const dim3 g((unsigned)((p.dz + 127) / 128), (unsigned)p.dy, (unsigned)p.dx);
-    FoldTile ft{0, 0, 0};
-    if (fold) ft = FoldTile{fold->ty, fold->tz, fold->xl};
+    const dim3 g((unsigned)((p.dz / 2 + 1 + 127) / 128), (unsigned)p.dy, (unsigned)p.dx);
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density<S><<<g, 128, 0, st>>>(p, P, (const S *)h, f0, rho, ft);
+        k_density<S><<<g, 128, 0, st>>>(p, P, (const S *)h, f0, rho);
     });
     hook_end(hook, K_DENSITY, st);
 }
@@ -313,10 +311,9 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     });
     hook_end(hook, K_FUSED, st);
     hook_begin(hook, K_DENSITY, st);
-    const FoldTile ft{t.ty, t.tz, t.xl};
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density_batch<S><<<dim3((unsigned)max_dx, (unsigned)nbox), 256, 0, st>>>(params, boxes, 1 - P, ft);
+        k_density_batch<S><<<dim3((unsigned)max_dx, (unsigned)nbox), 256, 0, st>>>(params, boxes, 1 - P);
     });
     hook_end(hook, K_DENSITY, st);
 }

@@ -113,13 +113,6 @@ __device__ __forceinline__ void scatter_pops(const KParams<float> &p, int P, S *
 }
 
 // ------------------------------------------------------------ density ----
-// Offset of the neighbour x + e_q in the flat index, for nodes whose
-// neighbours need no periodic wrap.
-__device__ __forceinline__ long long nb_off(int q, int plane, int dz)
-{
-    return (long long)cx(q) * plane + (long long)cy(q) * dz + cz(q);
-}
-
 // Is every node of the z-range [z0, z0+tz) and all its +-1 neighbours a fluid
 // node that needs no z wrap?
 __device__ __forceinline__ bool z_interior(const KParams<float> &p, int z0, int tz)
@@ -127,48 +120,17 @@ __device__ __forceinline__ bool z_interior(const KParams<float> &p, int z0, int 
     return p.wall_mode == 1 ? (z0 >= 4 && z0 + tz <= p.dz - 4) : (z0 >= 1 && z0 + tz <= p.dz - 1);
 }
 
-// Tile-interior node of the fused collide: its post-stream density is
-// computed inside the collide kernel (all 18 sources were collided by the
-// same CTA), so the density pass skips it.
-struct FoldTile {
-    int ty, tz, xl;  // 0 = fold off: the density pass computes every node
-};
-__device__ __forceinline__ bool fold_interior(const KParams<float> &p, const FoldTile &t, int i, int j, int k)
-{
-    if (t.xl <= 0) return false;
-    const int x0 = (i / t.xl) * t.xl, x1 = min(x0 + t.xl, p.dx);
-    const int y0 = (j / t.ty) * t.ty, yn = min(t.ty, p.dy - y0);
-    const int z0 = (k / t.tz) * t.tz, zn = min(t.tz, p.dz - z0);
-    const int ly = j - y0, lz = k - z0;
-    return i >= x0 + 1 && i <= x1 - 2 && ly >= 1 && ly <= yn - 2 && lz >= 1 && lz <= zn - 2;
-}
-
 // rho = sum of the post-stream populations (MacroCalculate's density,
 // FluidCuda.cu:357-361) on fluid nodes: r = f0, then r += f_q for q = 1..18
-// in order, every term decoded by decode_pop.  Grid: (z blocks, dy, dx).
+// in order, each term decoded by decode_pop.  The general path, for nodes
+// next to a wall or a periodic edge.
 template <class S>
 __device__ __forceinline__ void density_node(const KParams<float> &p, int P, const S *__restrict__ h,
-                                             const float *__restrict__ f0, float *__restrict__ rho,
-                                             const FoldTile &fold, int i, int j, int k)
+                                             const float *__restrict__ f0, float *__restrict__ rho, int i, int j,
+                                             int k)
 {
     if (solid_k(p.wall_mode, k, p.dz)) return;
-    if (fold_interior(p, fold, i, j, k)) return;
-    const int plane = p.dy * p.dz;
     const long long I = ((long long)i * p.dy + j) * p.dz + k;
-    const long long n = p.n;
-    const bool fast = i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy &&
-                      (p.wall_mode == 1 ? (k >= 4 && k <= p.dz - 5) : (k >= 1 && k + 1 < p.dz));
-    if (fast) {
-        float r = f0[I];
-#pragma unroll
-        for (int q = 1; q < Q; ++q) {
-            const long long src = I - nb_off(q, plane, p.dz);
-            const S hv = P == 0 ? h[(long long)(q - 1) * n + I] : h[(long long)(opp(q) - 1) * n + src];
-            r = __fadd_rn(r, decode_pop<S>(q, hv, __ldg(f0 + src)));
-        }
-        rho[I] = r;
-        return;
-    }
     float f[Q];
     gather_pops<S>(p, P, h, f0, i, j, k, I, f);
     float r = f[0];
@@ -177,14 +139,112 @@ __device__ __forceinline__ void density_node(const KParams<float> &p, int P, con
     rho[I] = r;
 }
 
+// Two stored values of consecutive nodes as a float pair: one vector load
+// when the first index is even, two scalar loads otherwise.
+template <class S>
+__device__ __forceinline__ float2 load_pair(const S *__restrict__ ptr, bool even);
+template <>
+__device__ __forceinline__ float2 load_pair<float>(const float *__restrict__ ptr, bool even)
+{
+    return even ? *reinterpret_cast<const float2 *>(ptr) : make_float2(ptr[0], ptr[1]);
+}
+template <>
+__device__ __forceinline__ float2 load_pair<__half>(const __half *__restrict__ ptr, bool even)
+{
+    return even ? __half22float2(*reinterpret_cast<const __half2 *>(ptr))
+                : make_float2(__half2float(ptr[0]), __half2float(ptr[1]));
+}
+template <>
+__device__ __forceinline__ float2 load_pair<__nv_bfloat16>(const __nv_bfloat16 *__restrict__ ptr, bool even)
+{
+    return even ? __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(ptr))
+                : make_float2(__bfloat162float(ptr[0]), __bfloat162float(ptr[1]));
+}
+
+// Is node k of a column one whose 18 sources are fluid nodes with no z wrap?
+__device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
+{
+    return p.wall_mode == 1 ? (k >= 4 && k <= p.dz - 5) : (k >= 1 && k <= p.dz - 2);
+}
+
+// Paired density of nodes I and I + 1 (I even, both with plain sources):
+// r += w_q h_q, then r += (w_q / w_0) a_q, q in order, in paired FP32.  With
+// an even DZ every pair of loads has a parity known at compile time (node
+// index and N even, so it is that of cz(q)) and aligned pairs are vector
+// loads; otherwise all moving-population and anchor loads are scalar.  Every
+// load is issued before the first add so their latencies overlap.
+template <class S, int P, bool EVEN>
+__device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const S *__restrict__ h,
+                                                  const float *__restrict__ f0, float *__restrict__ rho,
+                                                  long long I)
+{
+    const long long n = p.n;
+    const long long plane = (long long)p.dy * p.dz;
+    float2 hv[Q - 1], a[Q - 1];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        const long long off = cx(q) * plane + cy(q) * (long long)p.dz + cz(q);
+        const long long src = I - off;
+        const long long hi = P == 0 ? (long long)(q - 1) * n + I : (long long)(opp(q) - 1) * n + src;
+        const bool odd_off = (cz(q) & 1) != 0;
+        hv[q - 1] = load_pair<S>(h + hi, EVEN && (P == 0 || !odd_off));
+        a[q - 1] = load_pair<float>(f0 + src, EVEN && !odd_off);
+    }
+    float2 r = *reinterpret_cast<const float2 *>(f0 + I);
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        const float w = wgt<float>(q), rw = ratio0(q);
+        r = __ffma2_rn(make_float2(w, w), hv[q - 1], r);
+        r = __ffma2_rn(make_float2(rw, rw), a[q - 1], r);
+    }
+    *reinterpret_cast<float2 *>(rho + I) = r;
+}
+
+// Density of the nodes k0 and k0 + 1 of column (i, j) (either may lie
+// outside [0, dz)); the node index of k0 is even (see pair_k0).  Pairs next
+// to a wall or a periodic edge take the general per-node path.
+template <class S>
+__device__ __forceinline__ void density_pair(const KParams<float> &p, int P, const S *__restrict__ h,
+                                             const float *__restrict__ f0, float *__restrict__ rho, int i, int j,
+                                             int k0)
+{
+    const bool in0 = k0 >= 0 && k0 < p.dz, in1 = k0 + 1 >= 0 && k0 + 1 < p.dz;
+    const bool fast = in0 && in1 && i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy && z_plain(p, k0) &&
+                      z_plain(p, k0 + 1);
+    if (!fast) {
+        if (in0) density_node<S>(p, P, h, f0, rho, i, j, k0);
+        if (in1) density_node<S>(p, P, h, f0, rho, i, j, k0 + 1);
+        return;
+    }
+    const long long I = ((long long)i * p.dy + j) * p.dz + k0;
+    if ((p.dz & 1) == 0) {
+        if (P == 0) density_pair_fast<S, 0, true>(p, h, f0, rho, I);
+        else density_pair_fast<S, 1, true>(p, h, f0, rho, I);
+    } else {
+        if (P == 0) density_pair_fast<S, 0, false>(p, h, f0, rho, I);
+        else density_pair_fast<S, 1, false>(p, h, f0, rho, I);
+    }
+}
+
+// First node of the pair thread t of column (i, j) handles: pairs start on
+// even node indices, so a column whose first index is odd begins with a lone
+// node (k0 = -1).
+__device__ __forceinline__ int pair_k0(const KParams<float> &p, int i, int j, int t)
+{
+    const long long base = ((long long)i * p.dy + j) * p.dz;
+    return 2 * t - (int)(base & 1);
+}
+__device__ __forceinline__ int pairs_per_column(int dz) { return dz / 2 + 1; }
+
+// Grid: (pair blocks, dy, dx); thread t of a column handles one pair.
 template <class S>
 __global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const S *__restrict__ h,
-                                                 const float *__restrict__ f0, float *__restrict__ rho,
-                                                 FoldTile fold)
+                                                 const float *__restrict__ f0, float *__restrict__ rho)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= p.dz) return;
-    density_node<S>(p, P, h, f0, rho, fold, blockIdx.z, blockIdx.y, k);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= pairs_per_column(p.dz)) return;
+    const int i = blockIdx.z, j = blockIdx.y;
+    density_pair<S>(p, P, h, f0, rho, i, j, pair_k0(p, i, j, t));
 }
 
 // --------------------------------------------------------- fused step ----
@@ -206,20 +266,13 @@ struct FusedGeom {
     static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
     static constexpr int RM_PAIRS = 7 * MY * MZ;
     static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
-    static constexpr int TAB_INTS = RY + RZ;
+    static constexpr int TAB_INTS = 2 * RY + RZ;
     static constexpr size_t BASE_BYTES = sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
                                          sizeof(float) * F0_FLOATS + sizeof(int) * TAB_INTS;
-    // post-collision ring: planes x-3 .. x, each 18 stored moving populations
-    // (S) and the new rest population (float) per node
-    template <class S>
-    static constexpr size_t pc_bytes()
-    {
-        return 4 * (size_t)TY * TZ * (18 * sizeof(S) + sizeof(float));
-    }
     template <class S>
     static constexpr size_t bytes()
     {
-        return ((BASE_BYTES + 15) / 16) * 16 + pc_bytes<S>();
+        return ((BASE_BYTES + 15) / 16) * 16;
     }
 };
 
@@ -251,9 +304,8 @@ __device__ __forceinline__ int mod_small(int t, int m)
 template <class S, int TY, int TZ, int L>
 __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__restrict__ h,
                                            const float *__restrict__ f0c, float *__restrict__ f0n,
-                                           const float *__restrict__ rho, float *__restrict__ rho_next,
-                                           const int z0, const int y0, const int x0, const int xl,
-                                           float4 *smem4)
+                                           const float *__restrict__ rho, const int z0, const int y0,
+                                           const int x0, const int xl, float4 *smem4)
 {
     using G = FusedGeom<TY, TZ, L>;
     constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
@@ -264,44 +316,47 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
     float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
     int *tabY = reinterpret_cast<int *>(sf0 + G::F0_FLOATS);
     int *tabZ = tabY + RY;
-    unsigned char *pc_base = reinterpret_cast<unsigned char *>(smem4) + ((G::BASE_BYTES + 15) / 16) * 16;
-    constexpr int NTILE = TY * TZ;
-    // ring slot r: S h[18][NTILE] followed by float f0[NTILE]
-    auto pc_h = [&](int slot) { return reinterpret_cast<S *>(pc_base + (size_t)slot * NTILE * (18 * sizeof(S) + 4)); };
-    auto pc_f0 = [&](int slot) { return reinterpret_cast<float *>(pc_h(slot) + 18 * NTILE); };
+    int *tabYdz = tabZ + RZ;  // wrapped y row times dz
 
     const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
     const int x1 = min(x0 + xl, p.dx);
-    const int plane = p.dy * p.dz;
-    const long long n = p.n;
+    // node indices are 32-bit (the FUSED scheme keeps N below 2^32); slot q of
+    // node I is h + q * n + I with a 64-bit product
+    const unsigned plane = (unsigned)(p.dy * p.dz);
+    const unsigned n = (unsigned)p.n;
+    auto slot = [&](int q, unsigned idx) -> S * { return h + (size_t)n * (unsigned)q + idx; };
     const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
     const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
 
     // wrapped y / z coordinates of the halo rows and columns
     for (int e = threadIdx.x; e < RY + RZ; e += NT) {
-        if (e < RY) tabY[e] = wrap_small(y0 - RH + e, p.dy);
-        else tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+        if (e < RY) {
+            tabY[e] = wrap_small(y0 - RH + e, p.dy);
+            tabYdz[e] = tabY[e] * p.dz;
+        } else {
+            tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+        }
     }
     __syncthreads();
 
     auto issue_rho = [&](int xlog) {
-        const long long base = (long long)wrapm(xlog, p.dx) * p.dy;
+        const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = srho + ring_slot(xlog, NR) * (RY * RZ);
         for (int e = threadIdx.x; e < RY * RZ; e += NT) {
             const int ly = e / RZ, lz = e - ly * RZ;
-            cp_async4(dst + e, rho + (base + tabY[ly]) * p.dz + tabZ[lz]);
+            cp_async4(dst + e, src + (unsigned)(tabYdz[ly] + tabZ[lz]));
         }
     };
     auto issue_f0 = [&](int xlog) {
-        const long long base = (long long)wrapm(xlog, p.dx) * p.dy;
+        const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = sf0 + ring_slot(xlog, 4) * (AY * AZ);
         for (int e = threadIdx.x; e < AY * AZ; e += NT) {
             const int ly = e / AZ, lz = e - ly * AZ;
-            cp_async4(dst + e, f0c + (base + tabY[ly + RH - 1]) * p.dz + tabZ[lz + RH - 1]);
+            cp_async4(dst + e, src + (unsigned)(tabYdz[ly + RH - 1] + tabZ[lz + RH - 1]));
         }
     };
     auto comp_mu = [&](int xlog) {
-        const int gx = wrapm(xlog, p.dx);
+        const int gx = wrap_small(xlog, p.dx);
         float2 *dst = srm + ring_slot(xlog, 7) * (MY * MZ);
         const float *rc = srho + ring_slot(xlog, NR) * (RY * RZ);
         const float *rm1 = srho + ring_slot(xlog - 1, NR) * (RY * RZ);
@@ -316,7 +371,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             const float r0 = rc[c];
             const int gz = tabZ[mz + L];
             if (solid_k(p.wall_mode, gz, p.dz)) {
-                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : (long long)p.dx * p.dy) + (long long)gx * p.dy + tabY[my + L]]);
+                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : p.dx * p.dy) + gx * p.dy + tabY[my + L]]);
                 continue;
             }
             float lap;
@@ -344,50 +399,25 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
     // moving populations of one node of plane x into registers (A-A read slots)
     auto fetch = [&](int x, S hv[Q - 1]) {
         if (!active) return;
-        const int gx = wrapm(x, p.dx);
-        const long long I = ((long long)gx * p.dy + gy) * p.dz + gz;
+        const int gx = wrap_small(x, p.dx);
+        const unsigned I = (unsigned)gx * plane + (unsigned)(gy * p.dz + gz);
         if (P == 0) {
 #pragma unroll
-            for (int q = 1; q < Q; ++q) hv[q - 1] = h[(long long)(q - 1) * n + I];
+            for (int q = 1; q < Q; ++q) hv[q - 1] = *slot(q - 1, I);
         } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
 #pragma unroll
-            for (int q = 1; q < Q; ++q) hv[q - 1] = h[(long long)(opp(q) - 1) * n + I - nb_off(q, plane, p.dz)];
+            for (int q = 1; q < Q; ++q)
+                hv[q - 1] = *slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
         } else {
 #pragma unroll
             for (int q = 1; q < Q; ++q) {
                 const int si = wrap1(gx - cx(q), p.dx), sj = wrap1(gy - cy(q), p.dy), sk = wrap1(gz - cz(q), p.dz);
                 if (solid_k(p.wall_mode, sk, p.dz))
-                    hv[q - 1] = h[(long long)(q - 1) * n + I];
+                    hv[q - 1] = *slot(q - 1, I);
                 else
-                    hv[q - 1] = h[(long long)(opp(q) - 1) * n + ((long long)si * p.dy + sj) * p.dz + sk];
+                    hv[q - 1] = *slot(opp(q) - 1, (unsigned)si * plane + (unsigned)(sj * p.dz + sk));
             }
         }
-    };
-
-    // Post-stream density of the tile-interior nodes of plane xf, from the
-    // post-collision ring (planes xf-1 .. xf+1): the same decode and the same
-    // summation order as k_density, so the result is bit-identical.
-    const int yn = min(TY, p.dy - y0), zn = min(TZ, p.dz - z0);
-    auto fold_density = [&](int xf) {
-        if (!(active && ty >= 1 && ty <= yn - 2 && tz >= 1 && tz <= zn - 2)) return;
-        const int sb[3] = {ring_slot(xf - 1, 4), ring_slot(xf, 4), ring_slot(xf + 1, 4)};
-        const int me = threadIdx.x;
-        float r = pc_f0(sb[1])[me];
-#pragma unroll
-        for (int q = 1; q < Q; ++q) {
-            const int sk = gz - cz(q);
-            const bool ss = p.wall_mode == 1 && (sk < 3 || sk > p.dz - 4);
-            float v;
-            if (ss) {
-                v = decode_pop<S>(q, pc_h(sb[1])[(opp(q) - 1) * NTILE + me], pc_f0(sb[1])[me]);
-            } else {
-                const int src = me - cy(q) * TZ - cz(q);
-                const int slot = sb[1 - cx(q)];
-                v = decode_pop<S>(q, pc_h(slot)[(q - 1) * NTILE + src], pc_f0(slot)[src]);
-            }
-            r = __fadd_rn(r, v);
-        }
-        rho_next[((long long)wrapm(xf, p.dx) * p.dy + gy) * p.dz + gz] = r;
     };
 
     // prologue: mu(x0-3 .. x0+2); f0(x0-1 .. x0+1) and rho(x0+3+L) in flight
@@ -425,7 +455,6 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
         cp_async_commit();
         S hn[Q - 1];
         if (x + 1 < x1) fetch(x + 1, hn);
-        if (x - 2 >= x0 + 1) fold_density(x - 2);
         comp_mu(x + 3);
         __syncthreads();
         if (active) {
@@ -503,43 +532,33 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             }
 
             // encode against this node's new rest population and stream
-            const int gx = wrapm(x, p.dx);
-            const long long I = ((long long)gx * p.dy + gy) * p.dz + gz;
+            const int gx = wrap_small(x, p.dx);
+            const unsigned I = (unsigned)gx * plane + (unsigned)(gy * p.dz + gz);
             const float an = f[0];
             f0n[I] = an;
-            // keep the stored values for the in-tile density of this plane
-            {
-                const int sl = ring_slot(x, 4);
-                S *ph = pc_h(sl);
-                pc_f0(sl)[threadIdx.x] = an;
-#pragma unroll
-                for (int q = 1; q < Q; ++q) ph[(q - 1) * NTILE + threadIdx.x] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
-            }
             if (P == 0) {
 #pragma unroll
-                for (int q = 1; q < Q; ++q)
-                    h[(long long)(opp(q) - 1) * n + I] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                for (int q = 1; q < Q; ++q) *slot(opp(q) - 1, I) = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
             } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
 #pragma unroll
                 for (int q = 1; q < Q; ++q)
-                    h[(long long)(q - 1) * n + I + nb_off(q, plane, p.dz)] = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                    *slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))) =
+                        f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
             } else {
 #pragma unroll
                 for (int q = 1; q < Q; ++q) {
                     const S v = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
                     const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy), dk = wrap1(gz + cz(q), p.dz);
                     if (solid_k(p.wall_mode, dk, p.dz))
-                        h[(long long)(opp(q) - 1) * n + I] = v;
+                        *slot(opp(q) - 1, I) = v;
                     else
-                        h[(long long)(q - 1) * n + ((long long)di * p.dy + dj) * p.dz + dk] = v;
+                        *slot(q - 1, (unsigned)di * plane + (unsigned)(dj * p.dz + dk)) = v;
                 }
             }
         }
 #pragma unroll
         for (int q = 0; q < Q - 1; ++q) hv[q] = hn[q];
     }
-    __syncthreads();
-    if (x1 - 2 >= x0 + 1) fold_density(x1 - 2);
     cp_async_wait_all();
 }
 
@@ -547,12 +566,11 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
 template <class S, int TY, int TZ, int L>
 __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
     k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
-                    float *__restrict__ f0n, const float *__restrict__ rho, float *__restrict__ rho_next,
-                    int xl)
+                    float *__restrict__ f0n, const float *__restrict__ rho, int xl)
 {
     extern __shared__ float4 smem4[];
-    fused_tile<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, rho_next, blockIdx.x * TZ, blockIdx.y * TY,
-                             blockIdx.z * xl, xl, smem4);
+    fused_tile<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
+                             smem4);
 }
 
 // Many boxes in one persistent launch: each CTA takes (box, z tile, y tile,
@@ -587,17 +605,17 @@ __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], bx.rho[1 - P],
-                                 ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
+        fused_tile<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ, ytile * TY,
+                                 chunk * xl, xl, smem4);
         __syncthreads();
     }
 }
 
-// Batched density pass: one block per (box, x plane), threads over the plane.
+// Batched density pass: one block per (box, x plane), threads over the
+// plane's node pairs (the pairing of k_density).
 template <class S>
 __global__ void __launch_bounds__(256) k_density_batch(const KParams<float> *__restrict__ params,
-                                                       const BatchBox *__restrict__ boxes, int P,
-                                                       FoldTile fold)
+                                                       const BatchBox *__restrict__ boxes, int P)
 {
     const int b = blockIdx.y;
     const KParams<float> &p = params[b];
@@ -607,10 +625,11 @@ __global__ void __launch_bounds__(256) k_density_batch(const KParams<float> *__r
     const S *h = (const S *)bx.h;
     const float *f0 = bx.f0[P];
     float *rho = bx.rho[P];
-    const int nplane = p.dy * p.dz;
+    const int per_col = pairs_per_column(p.dz);
+    const int nplane = p.dy * per_col;
     for (int e = threadIdx.x; e < nplane; e += blockDim.x) {
-        const int j = e / p.dz, k = e - j * p.dz;
-        density_node<S>(p, P, h, f0, rho, fold, i, j, k);
+        const int j = e / per_col, t = e - j * per_col;
+        density_pair<S>(p, P, h, f0, rho, i, j, pair_k0(p, i, j, t));
     }
 }
 

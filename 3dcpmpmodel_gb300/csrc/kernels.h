@@ -58,15 +58,12 @@ void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d
 // Wall extrapolation on rho; every value written is mirrored into
 // rho_mirror when it is non-null (the other density buffer).
 void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, cudaStream_t st, LaunchHook *hook);
-// The fused collide reads rho (this step's density) and writes the next
-// step's density of its tile-interior nodes into rho_next.
+// The fused collide reads rho, this step's density (wall layers included).
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, float *rho_next, cudaStream_t st,
-                          LaunchHook *hook);
-// Density of the post-stream populations at parity P.  With fold != null,
-// the nodes the fused collide with that tile already wrote are skipped.
+                          const float *f0c, float *f0n, const float *rho, cudaStream_t st, LaunchHook *hook);
+// Density of the post-stream populations at parity P, every fluid node.
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
-                          const float *f0, float *rho, const FusedTile *fold, cudaStream_t st, LaunchHook *hook);
+                          const float *f0, float *rho, cudaStream_t st, LaunchHook *hook);
 // One time step of every box of a batch: batched wall passes, the persistent
 // fused collide over all (box, tile, chunk) work items, the batched density
 // pass.  params/boxes are device arrays of nbox entries; counter is one
