@@ -6,7 +6,8 @@
 on the bottom wall, FP32 PLAIN scheme; J = sum_fluid (rho^T - target)^2 with
 the target from a different seeded smooth 96 x 96 wall field.  Prints one
 JSON line: forward time, adjoint time (its own checkpointed forward, the
-segment replays and the reverse sweep), their ratio, and with --fd the FP64
+segment replays and the reverse sweep), their ratio, the per-kernel device time
+of a separately timed adjoint pass, and with --fd the FP64
 adjoint against central differences (h = 1e-3) for kappa and the two largest
 wall-gradient entries, plus the FP32-vs-FP64 gradient difference.
 """
@@ -71,11 +72,18 @@ def main():
     loss, gw, gk = s.adjoint(a.steps, target)
     t_adj = time.perf_counter() - t0
     s.close()
+    # per-kernel device time of one more adjoint pass (events around every launch)
+    s = ag._solver(st, w0, 0.01)
+    s.kernel_timing(True)
+    s.adjoint(a.steps, target)
+    kt = {k: {"launches": int(v[0]), "ms": round(v[1], 3)} for k, v in s.kernel_times().items()}
+    s.close()
     out = {"metric": "adjoint time / forward time", "value": round(t_adj / t_fwd, 3),
            "forward_s": round(t_fwd, 4), "adjoint_s": round(t_adj, 4),
            "backward_over_forward": round((t_adj - t_fwd) / t_fwd, 3),
            "config": {"grid": [L, L, L], "steps": a.steps, "storage": "f32", "checkpoint_every": "ceil(sqrt(T))"},
-           "loss": loss, "grad_kappa": gk, "grad_wall_norm": float(np.linalg.norm(gw))}
+           "loss": loss, "grad_kappa": gk, "grad_wall_norm": float(np.linalg.norm(gw)),
+           "kernel_ms_timed_pass": kt}
     if a.fd:
         st64 = setup("f64", L, L / 4)
         target64 = target

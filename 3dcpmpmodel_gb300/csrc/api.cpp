@@ -1240,7 +1240,7 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
 {
     const size_t n = (size_t)h->n, np = (size_t)h->p.dx * h->p.dy;
     const size_t state = 23 * n;    // checkpoint: f (19N) | rho (N) | u (3N)
-    const size_t sstate = 27 * n;   // segment state: f | rho | u | mu (N) | F (3N)
+    const size_t sstate = 29 * n;   // segment state: f | rho | u | grad mu (3N) | F (3N)
     const int nck = (T + S - 1) / S;
     std::vector<void *> mem;
     auto alloc = [&](void **p, size_t bytes, const char *what) -> cpmp_status {
@@ -1252,7 +1252,7 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
         for (void *q : mem) cudaFree(q);
         mem.clear();
     };
-    R *ck = nullptr, *seg = nullptr, *rr = nullptr, *mur = nullptr, *Fr = nullptr, *mvr = nullptr;
+    R *ck = nullptr, *seg = nullptr, *mvr = nullptr, *mus = nullptr;
     double *target = nullptr;
     AdjBufs<R> b{};
     const KParams<R> kp = make_kparams<R>(h);
@@ -1266,14 +1266,12 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     }
     ALLOC(ck, (size_t)nck * state * sizeof(R), "adjoint checkpoints");
     ALLOC(seg, (size_t)S * sstate * sizeof(R), "adjoint segment");
-    ALLOC(rr, n * sizeof(R), "adjoint rho");
-    ALLOC(mur, n * sizeof(R), "adjoint mu");
-    ALLOC(Fr, 3 * n * sizeof(R), "adjoint F");
     ALLOC(mvr, 3 * n * sizeof(R), "adjoint mv");
+    ALLOC(mus, n * sizeof(R), "adjoint mu");
     ALLOC(target, n * sizeof(double), "adjoint target");
     ALLOC(b.lamp, 19 * n * sizeof(R), "lambda partial");
     ALLOC(b.lamp_next, 19 * n * sizeof(R), "lambda partial");
-    ALLOC(b.lamF, 3 * n * sizeof(R), "lambda F");
+    ALLOC(b.lamF, 4 * n * sizeof(R), "lambda F");
     ALLOC(b.lammu, n * sizeof(R), "lambda mu");
     ALLOC(b.lamrho, n * sizeof(R), "lambda rho");
     ALLOC(b.lamrho_next, n * sizeof(R), "lambda rho");
@@ -1291,10 +1289,11 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
         cudaMemcpyAsync(dst + 19 * n, h->rho, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(dst + 20 * n, h->u, 3 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
     };
+    LaunchHook *hook = h->timing ? h->hook.get() : nullptr;
     // forward, checkpoint every S steps (the handle's own state advances to T)
     for (int t = 0; t < T; ++t) {
         if (t % S == 0) save(ck + (size_t)(t / S) * state);
-        launch_one_step(h, nullptr);
+        launch_one_step(h, hook);
     }
     adj_launch_loss<R>(kp, h->type, (const R *)h->rho, target, b, st);
     CK(cudaGetLastError());
@@ -1302,26 +1301,22 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     for (int kseg = nck - 1; kseg >= 0; --kseg) {
         const int n0 = kseg * S, n1 = std::min(n0 + S, T), len = n1 - n0;
         cudaMemcpyAsync(seg, ck + (size_t)kseg * state, state * sizeof(R), cudaMemcpyDeviceToDevice, st);
-        // replay the forward inside the segment; the step from state m-1 to m
-        // evaluates mu and F of state m-1 straight into its segment slot
+        // replay the forward inside the segment: the step from state m-1 to m
+        // extrapolates the wall layers of state m-1's density in place and
+        // leaves its grad mu and F in its slot, so each slot ends up holding
+        // what the reverse step needs (walled rho, u, grad mu, F)
         for (int m = 1; m < len; ++m) {
             R *prev = seg + (size_t)(m - 1) * sstate, *cur = seg + (size_t)m * sstate;
-            cudaMemcpyAsync(cur + 19 * n, prev + 19 * n, 4 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            plain_launch_step<R, R>(kp, h->type, cur + 19 * n, prev + 23 * n, cur + 20 * n, prev + 24 * n, mvr,
-                                    prev, cur, st, nullptr);
+            plain_launch_step_split<R, R>(kp, h->type, prev + 19 * n, mus, prev + 20 * n, prev + 26 * n, mvr, prev,
+                                          cur, cur + 19 * n, cur + 20 * n, prev + 23 * n, st, hook);
         }
-        {   // the last state of the segment is never stepped from: its mu, F
+        {   // the last state of the segment is never stepped from
             R *last = seg + (size_t)(len - 1) * sstate;
-            cudaMemcpyAsync(rr, last + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            plain_launch_mu_force<R>(kp, h->type, rr, last + 23 * n, last + 24 * n, st);
+            plain_launch_mu_force<R>(kp, h->type, last + 19 * n, mus, last + 26 * n, st, last + 23 * n);
         }
         for (int t = n1 - 1; t >= n0; --t) {
             const R *stt = seg + (size_t)(t - n0) * sstate;
-            // density of step t with its wall layers (the stored copy's solid
-            // layers belong to the step before)
-            cudaMemcpyAsync(rr, stt + 19 * n, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
-            plain_launch_wall<R>(kp, rr, st);
-            adj_launch_step<R>(kp, h->type, rr, stt + 20 * n, stt + 23 * n, stt + 24 * n, b, st);
+            adj_launch_step<R>(kp, h->type, stt + 19 * n, stt + 20 * n, stt + 23 * n, stt + 26 * n, b, st, hook);
             std::swap(b.lamp, b.lamp_next);
             std::swap(b.lamrho, b.lamrho_next);
         }

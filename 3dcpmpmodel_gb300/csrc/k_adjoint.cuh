@@ -15,13 +15,18 @@
 //       (bounce-back transposed), collision adjoint in moment space ->
 //       lamp (partial dJ/df), dJ/dF, the collision's dJ/drho
 //   R3  k_adj_force   : dJ/dmu(y) = sum_a G_a(rho lamF_a)(y),
-//       dJ/drho(y) += -sum_a G_a(lamF_a)(y)/3 - lamF(y).G(mu)(y)
+//       dJ/drho(y) += -sum_a G_a(lamF_a)(y)/3 - lamF(y).G(mu)(y); R2 hands
+//       lamF over packed with rho, (lamF_x, lamF_y, lamF_z, rho) per node, so
+//       each stencil point is one vector load; G(mu) is the one the forward
+//       replay stored
 //       (the gradient stencils are antisymmetric, so their transpose is the
 //       negated stencil)
 //   R4  k_adj_mu      : dJ/drho(y) += K^2 mu0'(rho) lam_mu - ka Lap(lam_mu on
-//       fluid)(y) (the Laplacian is symmetric); dJ/dka += -sum lam_mu Lap(rho)
+//       fluid)(y) (the Laplacian is symmetric); dJ/dka += -sum lam_mu Lap(rho),
+//       products and sums in FP64
 //   R5  k_adj_wall    : wall layers back onto the first fluid layer (the
-//       6-point average is symmetric), dJ/dw += lam_mu on the solid layers
+//       6-point average is symmetric), dJ/dw += lam_mu on the solid layers;
+//       one launch for all three layers
 //   (R6, dJ/df^n_q = lamp_q + lamrho, is folded into the next R2's gather)
 // The K1/K2 pressure-tensor term is not differentiated (callers get
 // CPMP_ERR_UNSUPPORTED when it is active).
@@ -85,18 +90,38 @@ __device__ __forceinline__ void meq_adjoint(R rho, R vx, R vy, R vz, const R Aw[
                   Aw[15] * vx);
 }
 
+// Neighbour (i+a, j+b, k+c) of node I: plain offsets for nodes at least
+// `radius` away from every face (INTERIOR), periodic wrap otherwise.
+template <bool INTERIOR, class R>
+struct Nb {
+    const KParams<R> &p;
+    int i, j, k;
+    long long I, plane;
+    __device__ __forceinline__ long long operator()(int a, int b, int c) const
+    {
+        if (INTERIOR) return I + a * plane + (long long)b * p.dz + c;
+        return nid(p, wrap_off(i + a, p.dx), wrap_off(j + b, p.dy), wrap_off(k + c, p.dz));
+    }
+};
+template <class R>
+__device__ __forceinline__ bool interior_node(const KParams<R> &p, int i, int j, int k, int radius)
+{
+    return i >= radius && i < p.dx - radius && j >= radius && j < p.dy - radius && k >= radius && k < p.dz - radius;
+}
+
 // R2: collision + streaming adjoint (one thread per node, 3-D grid).
 template <class R>
 __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t *type, const R *rho,
                                                      const R *u, const R *F, const R *lamp_next,
-                                                     const R *lamrho_next, R *lamp, R *lamF, R *lamrho)
+                                                     const R *lamrho_next, R *lamp, Pack4<R> *lamF,
+                                                     R *lamrho)
 {
     NODE3D(p);
     const long long n = p.n;
     if (type[I] != FLUID) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) lamp[q * n + I] = R(0);
-        lamF[I] = lamF[I + n] = lamF[I + 2 * n] = R(0);
+        lamF[I] = Pack4<R>{R(0), R(0), R(0), rho[I]};
         lamrho[I] = R(0);
         return;
     }
@@ -105,12 +130,16 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     // back into slot opp(q) of this node
     R ls[Q];
     const R lr_here = lamrho_next[I];
+    auto gather = [&](auto nb) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const int ii = wrap_off(i + cx(q), p.dx), jj = wrap_off(j + cy(q), p.dy), kk = wrap_off(k + cz(q), p.dz);
-        const long long D = nid(p, ii, jj, kk);
-        ls[q] = type[D] == FLUID ? lamp_next[q * n + D] + lamrho_next[D] : lamp_next[opp(q) * n + I] + lr_here;
-    }
+        for (int q = 0; q < Q; ++q) {
+            const long long D = nb(cx(q), cy(q), cz(q));
+            ls[q] = type[D] == FLUID ? lamp_next[q * n + D] + lamrho_next[D] : lamp_next[opp(q) * n + I] + lr_here;
+        }
+    };
+    const long long plane = (long long)p.dy * p.dz;
+    if (interior_node(p, i, j, k, 1)) gather(Nb<true, R>{p, i, j, k, I, plane});
+    else gather(Nb<false, R>{p, i, j, k, I, plane});
     // mu* = M^-T lambda* = diag(1/norm) M lambda*
     R ms[Q];
     moments<R>(ls, ms);
@@ -136,9 +165,7 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     aux += av1x;
     auy += av1y;
     auz += av1z;
-    lamF[I] = av1x * ir;
-    lamF[I + n] = av1y * ir;
-    lamF[I + 2 * n] = av1z * ir;
+    lamF[I] = Pack4<R>{av1x * ir, av1y * ir, av1z * ir, r};
     a_rho -= (av1x * Fx + av1y * Fy + av1z * Fz) * ir * ir;
     // u = j / rho
     const R ajx = aux * ir, ajy = auy * ir, ajz = auz * ir;
@@ -157,95 +184,61 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     for (int q = 0; q < Q; ++q) lamp[q * n + I] = fm[q] + R(cx(q)) * ajx + R(cy(q)) * ajy + R(cz(q)) * ajz;
 }
 
-// R3: force adjoint (stencil gathers).
+// R3: force adjoint (stencil gathers of the packed (lamF, rho)).
 template <class R>
-__global__ void __launch_bounds__(128) k_adj_force(KParams<R> p, const uint8_t *type, const R *rho, const R *mu,
-                                                   const R *lamF, R *lammu, R *lamrho)
+__global__ void __launch_bounds__(128, 4) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
+                                                      const Pack4<R> *lamF, R *lammu, R *lamrho)
 {
     NODE3D(p);
     const long long n = p.n;
-    int a[7], b[7], c[7];
+    const long long plane = (long long)p.dy * p.dz;
+    auto body = [&](auto nb) {
+        // for each lattice line (sx, sy, sz) with weight vector w (2 e on the
+        // axes, e on the diagonals): sum_d c_d (v(+d) - v(-d)) of v = w . lamF
+        // and of rho v; only the nonzero components of w enter
+        R sm = R(0), sr = R(0);
+        auto acc = [&](auto SX, auto SY, auto SZ) {
+            constexpr int sx = decltype(SX)::value, sy = decltype(SY)::value, sz = decltype(SZ)::value;
+            constexpr int axis = (sx != 0) + (sy != 0) + (sz != 0) == 1;
+            constexpr int wx = axis ? 2 * sx : sx, wy = axis ? 2 * sy : sy, wz = axis ? 2 * sz : sz;
+            auto lw = [&](const Pack4<R> &v4) -> R {
+                R v = R(0);
+                if constexpr (wx != 0) v += R(wx) * v4.x;
+                if constexpr (wy != 0) v += R(wy) * v4.y;
+                if constexpr (wz != 0) v += R(wz) * v4.z;
+                return v;
+            };
 #pragma unroll
-    for (int d = -3; d <= 3; ++d) {
-        a[d + 3] = wrap_off(i + d, p.dx);
-        b[d + 3] = wrap_off(j + d, p.dy);
-        c[d + 3] = wrap_off(k + d, p.dz);
-    }
-    // for each lattice line (sx, sy, sz) with weight vector w (2 e on the
-    // axes, e on the diagonals): sum_d c_d (v(+d) - v(-d)) of v = w . lamF
-    // and of rho v; only the nonzero components of w are loaded
-    R gm = R(0), gr = R(0);
-    auto acc = [&](auto SX, auto SY, auto SZ) {
-        constexpr int sx = decltype(SX)::value, sy = decltype(SY)::value, sz = decltype(SZ)::value;
-        constexpr int axis = (sx != 0) + (sy != 0) + (sz != 0) == 1;
-        constexpr int wx = axis ? 2 * sx : sx, wy = axis ? 2 * sy : sy, wz = axis ? 2 * sz : sz;
-        auto lw = [&](long long P) -> R {
-            R v = R(0);
-            if constexpr (wx != 0) v += R(wx) * lamF[P];
-            if constexpr (wy != 0) v += R(wy) * lamF[P + n];
-            if constexpr (wz != 0) v += R(wz) * lamF[P + 2 * n];
-            return v;
+            for (int d = 1; d <= 3; ++d) {
+                const R cd = d == 1 ? R(45) : (d == 2 ? R(-9) : R(1));
+                const Pack4<R> vp = lamF[nb(sx * d, sy * d, sz * d)], vm = lamF[nb(-sx * d, -sy * d, -sz * d)];
+                const R lp = lw(vp), lm = lw(vm);
+                sm += cd * (vp.w * lp - vm.w * lm);
+                sr += cd * (lp - lm);
+            }
         };
-#pragma unroll
-        for (int d = 1; d <= 3; ++d) {
-            const R cd = d == 1 ? R(45) : (d == 2 ? R(-9) : R(1));
-            const long long P_ = nid(p, a[3 + sx * d], b[3 + sy * d], c[3 + sz * d]);
-            const long long M_ = nid(p, a[3 - sx * d], b[3 - sy * d], c[3 - sz * d]);
-            const R lp = lw(P_), lm = lw(M_);
-            gm += cd * (rho[P_] * lp - rho[M_] * lm);
-            gr += cd * (lp - lm);
+        using P1 = std::integral_constant<int, 1>;
+        using Z0 = std::integral_constant<int, 0>;
+        using M1 = std::integral_constant<int, -1>;
+        acc(P1{}, Z0{}, Z0{});
+        acc(Z0{}, P1{}, Z0{});
+        acc(Z0{}, Z0{}, P1{});
+        acc(P1{}, P1{}, Z0{});
+        acc(P1{}, M1{}, Z0{});
+        acc(P1{}, Z0{}, P1{});
+        acc(P1{}, Z0{}, M1{});
+        acc(Z0{}, P1{}, P1{});
+        acc(Z0{}, P1{}, M1{});
+        lammu[I] = sm / R(360);
+        R add = -sr / R(360) / R(3);
+        if (type[I] == FLUID) {  // grad(mu) of the forward step, stored by its replay
+            const Pack4<R> l = lamF[I];
+            add -= l.x * gm[I] + l.y * gm[I + n] + l.z * gm[I + 2 * n];
         }
+        lamrho[I] += add;
     };
-    using P1 = std::integral_constant<int, 1>;
-    using Z0 = std::integral_constant<int, 0>;
-    using M1 = std::integral_constant<int, -1>;
-    acc(P1{}, Z0{}, Z0{});
-    acc(Z0{}, P1{}, Z0{});
-    acc(Z0{}, Z0{}, P1{});
-    acc(P1{}, P1{}, Z0{});
-    acc(P1{}, M1{}, Z0{});
-    acc(P1{}, Z0{}, P1{});
-    acc(P1{}, Z0{}, M1{});
-    acc(Z0{}, P1{}, P1{});
-    acc(Z0{}, P1{}, M1{});
-    lammu[I] = gm / R(360);
-    R add = -gr / R(360) / R(3);
-    if (type[I] == FLUID) {
-        R g[3];
-        grad7_g(p, mu, i, j, k, g);
-        add -= lamF[I] * g[0] + lamF[I + n] * g[1] + lamF[I + 2 * n] * g[2];
-    }
-    lamrho[I] += add;
-}
-
-// Laplacians of an R field evaluated in FP64 (for the kappa gradient).
-template <class R>
-__device__ __forceinline__ double lap5_d(const KParams<R> &p, const R *x, int i, int j, int k)
-{
-    auto X = [&](int a, int b, int c) -> double { return (double)x[nid(p, a, b, c)]; };
-    const int im2 = wrap_off(i - 2, p.dx), im1 = wrap_off(i - 1, p.dx), ip1 = wrap_off(i + 1, p.dx),
-              ip2 = wrap_off(i + 2, p.dx);
-    const int jm2 = wrap_off(j - 2, p.dy), jm1 = wrap_off(j - 1, p.dy), jp1 = wrap_off(j + 1, p.dy),
-              jp2 = wrap_off(j + 2, p.dy);
-    const int km2 = wrap_off(k - 2, p.dz), km1 = wrap_off(k - 1, p.dz), kp1 = wrap_off(k + 1, p.dz),
-              kp2 = wrap_off(k + 2, p.dz);
-    return (-X(i, j, k) * 90.0 + (-X(im2, j, k) + X(im1, j, k) * 16.0 + X(ip1, j, k) * 16.0 - X(ip2, j, k)) +
-            (-X(i, jm2, k) + X(i, jm1, k) * 16.0 + X(i, jp1, k) * 16.0 - X(i, jp2, k)) +
-            (-X(i, j, km2) + X(i, j, km1) * 16.0 + X(i, j, kp1) * 16.0 - X(i, j, kp2))) /
-           12.0;
-}
-template <class R>
-__device__ __forceinline__ double lap7_d(const KParams<R> &p, const R *x, int i, int j, int k)
-{
-    auto X = [&](int a, int b, int c) -> double { return (double)x[nid(p, a, b, c)]; };
-    double s = -X(i, j, k) * 1470.0;
-#pragma unroll
-    for (int d = 1; d <= 3; ++d) {
-        const double w = d == 1 ? 270.0 : (d == 2 ? -27.0 : 2.0);
-        s += w * (X(wrap_off(i + d, p.dx), j, k) + X(wrap_off(i - d, p.dx), j, k) + X(i, wrap_off(j + d, p.dy), k) +
-                  X(i, wrap_off(j - d, p.dy), k) + X(i, j, wrap_off(k + d, p.dz)) + X(i, j, wrap_off(k - d, p.dz)));
-    }
-    return s / 180.0;
+    if (interior_node(p, i, j, k, 3)) body(Nb<true, R>{p, i, j, k, I, plane});
+    else body(Nb<false, R>{p, i, j, k, I, plane});
 }
 
 // R4: chemical-potential adjoint; per-block FP64 partials of dJ/dka.
@@ -259,50 +252,40 @@ __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *typ
     double gka = 0.0;
     if (k < p.dz) {
         const long long I = ((long long)i * p.dy + j) * p.dz + k;
-        // Laplacian of lam_mu restricted to fluid nodes (symmetric stencil)
-        auto lm = [&](int ii, int jj, int kk) -> R {
-            const long long J = nid(p, ii, jj, kk);
-            return type[J] == FLUID ? lammu[J] : R(0);
+        const long long plane = (long long)p.dy * p.dz;
+        auto body = [&](auto nb) {
+            // Laplacian of lam_mu restricted to fluid nodes (the stencil is
+            // symmetric), and the forward's Laplacian of rho for dJ/dka
+            auto lm = [&](int a, int b, int c) -> R {
+                const long long J = nb(a, b, c);
+                return type[J] == FLUID ? lammu[J] : R(0);
+            };
+            auto rr = [&](int a, int b, int c) -> R { return rho[nb(a, b, c)]; };
+            auto lap = [&](auto f) -> R {
+                if (p.lap_order == 7) {
+                    R s7 = -f(0, 0, 0) * R(1470);
+#pragma unroll
+                    for (int d = 1; d <= 3; ++d) {
+                        const R w = d == 1 ? R(270) : (d == 2 ? R(-27) : R(2));
+                        s7 += w * (f(d, 0, 0) + f(-d, 0, 0) + f(0, d, 0) + f(0, -d, 0) + f(0, 0, d) + f(0, 0, -d));
+                    }
+                    return s7 / R(180);
+                }
+                return (-f(0, 0, 0) * R(90) + (-f(-2, 0, 0) + f(-1, 0, 0) * R(16) + f(1, 0, 0) * R(16) - f(2, 0, 0)) +
+                        (-f(0, -2, 0) + f(0, -1, 0) * R(16) + f(0, 1, 0) * R(16) - f(0, 2, 0)) +
+                        (-f(0, 0, -2) + f(0, 0, -1) * R(16) + f(0, 0, 1) * R(16) - f(0, 0, 2))) /
+                       R(12);
+            };
+            R add = -p.ka * lap(lm);
+            if (type[I] == FLUID) {
+                const R r = rho[I];
+                add += p.kk * dmu0<R>(p.eos, p.A, p.B, p.T, r) * lammu[I];
+                gka = -(double)lammu[I] * (double)lap(rr);
+            }
+            lamrho[I] += add;
         };
-        R lap;
-        if (p.lap_order == 7) {
-            int a[7], b[7], c[7];
-#pragma unroll
-            for (int d = -3; d <= 3; ++d) {
-                a[d + 3] = wrap_off(i + d, p.dx);
-                b[d + 3] = wrap_off(j + d, p.dy);
-                c[d + 3] = wrap_off(k + d, p.dz);
-            }
-            lap = -lm(i, j, k) * R(1470);
-#pragma unroll
-            for (int d = 1; d <= 3; ++d) {
-                const R w = d == 1 ? R(270) : (d == 2 ? R(-27) : R(2));
-                lap += w * (lm(a[3 + d], j, k) + lm(a[3 - d], j, k) + lm(i, b[3 + d], k) + lm(i, b[3 - d], k) +
-                            lm(i, j, c[3 + d]) + lm(i, j, c[3 - d]));
-            }
-            lap /= R(180);
-        } else {
-            const int im2 = wrap_off(i - 2, p.dx), im1 = wrap_off(i - 1, p.dx), ip1 = wrap_off(i + 1, p.dx),
-                      ip2 = wrap_off(i + 2, p.dx);
-            const int jm2 = wrap_off(j - 2, p.dy), jm1 = wrap_off(j - 1, p.dy), jp1 = wrap_off(j + 1, p.dy),
-                      jp2 = wrap_off(j + 2, p.dy);
-            const int km2 = wrap_off(k - 2, p.dz), km1 = wrap_off(k - 1, p.dz), kp1 = wrap_off(k + 1, p.dz),
-                      kp2 = wrap_off(k + 2, p.dz);
-            lap = (-lm(i, j, k) * R(90) + (-lm(im2, j, k) + lm(im1, j, k) * R(16) + lm(ip1, j, k) * R(16) - lm(ip2, j, k)) +
-                   (-lm(i, jm2, k) + lm(i, jm1, k) * R(16) + lm(i, jp1, k) * R(16) - lm(i, jp2, k)) +
-                   (-lm(i, j, km2) + lm(i, j, km1) * R(16) + lm(i, j, kp1) * R(16) - lm(i, j, kp2))) /
-                  R(12);
-        }
-        R add = -p.ka * lap;
-        if (type[I] == FLUID) {
-            const R r = rho[I];
-            add += p.kk * dmu0<R>(p.eos, p.A, p.B, p.T, r) * lammu[I];
-            // the Laplacian of this term in FP64: it is a small difference of
-            // O(rho_l) values summed over every node and step
-            const double lr = p.lap_order == 7 ? lap7_d(p, rho, i, j, k) : lap5_d(p, rho, i, j, k);
-            gka = -(double)lammu[I] * lr;
-        }
-        lamrho[I] += add;
+        if (interior_node(p, i, j, k, 3)) body(Nb<true, R>{p, i, j, k, I, plane});
+        else body(Nb<false, R>{p, i, j, k, I, plane});
     }
     red[threadIdx.x] = gka;
     __syncthreads();
@@ -314,42 +297,65 @@ __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *typ
         ka_part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = red[0];
 }
 
-// R5: wall adjoint per column; pass 0 also gathers dJ/dw from the solid mu.
+// R5: wall adjoint in one launch.  The forward sets layer 2 = E(layer 3),
+// layer 1 = E(layer 2), layer 0 = E(layer 1) (or all three = E(layer 3) for
+// the single-layer rule), E = (2 centre + 4 xy-diagonal neighbours) / 6
+// with periodic wrap, which is symmetric (E^T = E).  Reversed:
+// lam1 += E(lam0), lam2 += E(lam1), lam3 += E(lam2).  A CTA owns a 16 x 16
+// tile of wall columns of one wall (blockIdx.z: 0 bottom, 1 top); it stages
+// the three solid layers' adjoints with halos 3, 2 and 1 in shared memory,
+// runs the chain there, and adds the result to the fluid layer next to the
+// wall (only that layer's adjoint is read afterwards).  dJ/dw gathers lam_mu
+// of the three solid layers.
+constexpr int WT = 16;  // wall tile edge (columns)
 template <class R>
-__global__ void k_adj_wall(KParams<R> p, int pass, const R *lammu, R *lamrho, double *gwall)
+__global__ void __launch_bounds__(256) k_adj_wall(KParams<R> p, const R *lammu, R *lamrho, double *gwall)
 {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= (long long)p.dx * p.dy) return;
-    const int i = (int)(c / p.dy), j = (int)(c % p.dy), D = p.dz;
-    // E^T = E: (2 centre + 4 xy-diagonal neighbours) / 6 of the adjoint layer
-    auto E = [&](int kk) -> R { return wall_extrap<R>(p, lamrho, i, j, kk); };
-    if (pass == 0) {
-        const long long np = (long long)p.dx * p.dy;
-        gwall[c] += (double)lammu[nid(p, i, j, 0)] + (double)lammu[nid(p, i, j, 1)] + (double)lammu[nid(p, i, j, 2)];
-        gwall[np + c] += (double)lammu[nid(p, i, j, D - 3)] + (double)lammu[nid(p, i, j, D - 2)] +
-                         (double)lammu[nid(p, i, j, D - 1)];
-    }
+    __shared__ R s0[WT + 6][WT + 6], s1[WT + 4][WT + 4], s2[WT + 2][WT + 2];
+    const bool top = blockIdx.z == 1;
+    const int D = p.dz;
+    const int kl0 = top ? D - 1 : 0, kl1 = top ? D - 2 : 1, kl2 = top ? D - 3 : 2, kf = top ? D - 4 : 3;
+    const int i0 = blockIdx.x * WT, j0 = blockIdx.y * WT;
+    auto col = [&](int a, int b, int k) -> long long {
+        return nid(p, wrap_off(a, p.dx), wrap_off(b, p.dy), k);
+    };
     if (p.complex_bc) {
-        // forward: L2 = E(L3), L1 = E(L2), L0 = E(L1)  ->  reverse in the opposite order
-        if (pass == 0) {
-            const R b = E(0), t = E(D - 1);
-            lamrho[nid(p, i, j, 1)] += b;
-            lamrho[nid(p, i, j, D - 2)] += t;
-        } else if (pass == 1) {
-            const R b = E(1), t = E(D - 2);
-            lamrho[nid(p, i, j, 2)] += b;
-            lamrho[nid(p, i, j, D - 3)] += t;
-        } else {
-            const R b = E(2), t = E(D - 3);
-            lamrho[nid(p, i, j, 3)] += b;
-            lamrho[nid(p, i, j, D - 4)] += t;
+        for (int e = threadIdx.x; e < (WT + 6) * (WT + 6); e += blockDim.x) {
+            const int a = e / (WT + 6), b = e % (WT + 6);
+            s0[a][b] = lamrho[col(i0 - 3 + a, j0 - 3 + b, kl0)];
+            if (a < WT + 4 && b < WT + 4) s1[a][b] = lamrho[col(i0 - 2 + a, j0 - 2 + b, kl1)];
+            if (a < WT + 2 && b < WT + 2) s2[a][b] = lamrho[col(i0 - 1 + a, j0 - 1 + b, kl2)];
         }
-    } else if (pass == 0) {
-        // forward: L0 = L1 = L2 = E(L3)
-        const R b = E(0) + E(1) + E(2), t = E(D - 1) + E(D - 2) + E(D - 3);
-        lamrho[nid(p, i, j, 3)] += b;
-        lamrho[nid(p, i, j, D - 4)] += t;
+        __syncthreads();
+        for (int e = threadIdx.x; e < (WT + 4) * (WT + 4); e += blockDim.x) {
+            const int a = e / (WT + 4) + 1, b = e % (WT + 4) + 1;  // centre in s0 coordinates
+            s1[a - 1][b - 1] += (s0[a][b] * R(2) + s0[a - 1][b - 1] + s0[a - 1][b + 1] + s0[a + 1][b - 1] +
+                                 s0[a + 1][b + 1]) / R(6);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < (WT + 2) * (WT + 2); e += blockDim.x) {
+            const int a = e / (WT + 2) + 1, b = e % (WT + 2) + 1;  // centre in s1 coordinates
+            s2[a - 1][b - 1] += (s1[a][b] * R(2) + s1[a - 1][b - 1] + s1[a - 1][b + 1] + s1[a + 1][b - 1] +
+                                 s1[a + 1][b + 1]) / R(6);
+        }
+        __syncthreads();
     }
+    const int a = threadIdx.x / WT, b = threadIdx.x % WT;
+    const int i = i0 + a, j = j0 + b;
+    if (i >= p.dx || j >= p.dy) return;
+    const long long np = (long long)p.dx * p.dy, c = (long long)i * p.dy + j;
+    gwall[(top ? np : 0) + c] += (double)lammu[nid(p, i, j, kl0)] + (double)lammu[nid(p, i, j, kl1)] +
+                                 (double)lammu[nid(p, i, j, kl2)];
+    R add;
+    if (p.complex_bc) {
+        add = (s2[a + 1][b + 1] * R(2) + s2[a][b] + s2[a][b + 2] + s2[a + 2][b] + s2[a + 2][b + 2]) / R(6);
+    } else {
+        auto Ls = [&](int aa, int bb) {
+            return lamrho[col(aa, bb, kl0)] + lamrho[col(aa, bb, kl1)] + lamrho[col(aa, bb, kl2)];
+        };
+        add = (Ls(i, j) * R(2) + Ls(i - 1, j - 1) + Ls(i - 1, j + 1) + Ls(i + 1, j - 1) + Ls(i + 1, j + 1)) / R(6);
+    }
+    lamrho[nid(p, i, j, kf)] += add;
 }
 
 // Loss J = sum over fluid nodes of (rho - target)^2 (FP64 partials) and the
@@ -410,23 +416,33 @@ void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, con
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.loss, 0);
 }
 
-// One reverse step.  rho/u/mu/F hold the forward intermediates of step n
-// (recomputed from f^n by the caller); (b.lamp_next, b.lamrho_next) =
-// dJ/df^{n+1} on entry, (b.lamp, b.lamrho) = dJ/df^n on exit.
+// One reverse step.  rho/u/gm/F hold the forward intermediates of step n
+// (density with its wall layers, velocity, grad mu, force; recomputed from
+// f^n by the caller); (b.lamp_next, b.lamrho_next) = dJ/df^{n+1} on entry,
+// (b.lamp, b.lamrho) = dJ/df^n on exit.
 template <class R>
-void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *mu, const R *F,
-                     AdjBufs<R> &b, cudaStream_t st)
+void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *gm, const R *F,
+                     AdjBufs<R> &b, cudaStream_t st, LaunchHook *hook)
 {
     const dim3 g = grid3(p, 128);
-    k_adj_collide<R><<<g, 128, 0, st>>>(p, type, rho, u, F, b.lamp_next, b.lamrho_next, b.lamp, b.lamF,
-                                        b.lamrho);
-    k_adj_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, b.lamF, b.lammu, b.lamrho);
+    Pack4<R> *lamF = reinterpret_cast<Pack4<R> *>(b.lamF);
+    hook_begin(hook, K_ADJ_COLLIDE, st);
+    k_adj_collide<R><<<g, 128, 0, st>>>(p, type, rho, u, F, b.lamp_next, b.lamrho_next, b.lamp, lamF, b.lamrho);
+    hook_end(hook, K_ADJ_COLLIDE, st);
+    hook_begin(hook, K_ADJ_FORCE, st);
+    k_adj_force<R><<<g, 128, 0, st>>>(p, type, gm, lamF, b.lammu, b.lamrho);
+    hook_end(hook, K_ADJ_FORCE, st);
+    hook_begin(hook, K_ADJ_MU, st);
     k_adj_mu<R><<<g, 128, 0, st>>>(p, type, rho, b.lammu, b.lamrho, b.ka_part);
+    hook_end(hook, K_ADJ_MU, st);
+    hook_begin(hook, K_ADJ_SUM, st);
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.gka, 1);
+    hook_end(hook, K_ADJ_SUM, st);
     if (p.wall_mode == 1) {
-        const long long np = (long long)p.dx * p.dy;
-        const unsigned gw = (unsigned)((np + 127) / 128);
-        for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) k_adj_wall<R><<<gw, 128, 0, st>>>(p, s, b.lammu, b.lamrho, b.gwall);
+        const dim3 gw((unsigned)((p.dx + WT - 1) / WT), (unsigned)((p.dy + WT - 1) / WT), 2);
+        hook_begin(hook, K_ADJ_WALL, st);
+        k_adj_wall<R><<<gw, WT * WT, 0, st>>>(p, b.lammu, b.lamrho, b.gwall);
+        hook_end(hook, K_ADJ_WALL, st);
     }
 }
 

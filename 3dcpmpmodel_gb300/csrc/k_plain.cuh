@@ -208,9 +208,10 @@ __global__ void k_chem_potential(KParams<R> p, const uint8_t *type, const R *rho
         mu[I] = p.kk * m0 - p.ka * lap5_g(p, rho, i, j, k);
 }
 
-// NonidealForce (FluidCuda.cu:431-441): F = -rho grad(mu) + grad(rho)/3
+// NonidealForce (FluidCuda.cu:431-441): F = -rho grad(mu) + grad(rho)/3;
+// grad(mu) is also stored when gm_out is non-null (the adjoint's replay).
 template <class R>
-__global__ void k_force(KParams<R> p, const uint8_t *type, const R *rho, const R *mu, R *F)
+__global__ void k_force(KParams<R> p, const uint8_t *type, const R *rho, const R *mu, R *F, R *gm_out)
 {
     NODE3D(p);
     if (type[I] != FLUID) return;
@@ -221,6 +222,11 @@ __global__ void k_force(KParams<R> p, const uint8_t *type, const R *rho, const R
     F[I] = -gm[0] * r + gr[0] / R(3);
     F[I + p.n] = -gm[1] * r + gr[1] / R(3);
     F[I + 2 * p.n] = -gm[2] * r + gr[2] / R(3);
+    if (gm_out) {
+        gm_out[I] = gm[0];
+        gm_out[I + p.n] = gm[1];
+        gm_out[I + 2 * p.n] = gm[2];
+    }
 }
 
 // GlobalCollide (FluidCuda.cu:311-347): MV, MRT + exact-difference forcing,
@@ -298,16 +304,20 @@ void plain_launch_init(const KParams<R> &p, const DropletDev &d, uint8_t *type, 
     k_init_plain<R, S><<<g, 256, 0, st>>>(p, d, type, rho, mu, u, f);
 }
 
+// One step with the density / velocity of step n read from (rho, u) and
+// those of step n+1 written to (rho_out, u_out); the wall layers are
+// extrapolated into rho in place and mu, F (and grad mu when gm_out is
+// non-null) are left in their buffers.
 template <class R, class S>
-void plain_launch_step(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *u, R *F, R *mv,
-                       const S *fc, S *fn, cudaStream_t st, LaunchHook *hook)
+void plain_launch_step_split(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, const R *u, R *F, R *mv,
+                             const S *fc, S *fn, R *rho_out, R *u_out, R *gm_out, cudaStream_t st,
+                             LaunchHook *hook)
 {
     const dim3 g = grid3(p, 128);
     if (p.wall_mode == 1) {
         const long long np = (long long)p.dx * p.dy;
         const unsigned gw = (unsigned)((np + 127) / 128);
-        const int passes = p.complex_bc ? 3 : 1;
-        for (int s = 0; s < passes; ++s) {
+        for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) {
             hook_begin(hook, K_WALL, st);
             k_wall_pass<R><<<gw, 128, 0, st>>>(p, s, rho, mu);
             hook_end(hook, K_WALL, st);
@@ -317,14 +327,22 @@ void plain_launch_step(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, 
     k_chem_potential<R><<<g, 128, 0, st>>>(p, type, rho, mu);
     hook_end(hook, K_MU, st);
     hook_begin(hook, K_FORCE, st);
-    k_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, F);
+    k_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, F, gm_out);
     hook_end(hook, K_FORCE, st);
     hook_begin(hook, K_COLLIDE, st);
     k_collide_plain<R, S><<<g, 128, 0, st>>>(p, type, rho, u, F, fc, fn, mv);
     hook_end(hook, K_COLLIDE, st);
     hook_begin(hook, K_MACRO, st);
-    k_macro<R, S><<<g, 128, 0, st>>>(p, type, fn, rho, u);
+    k_macro<R, S><<<g, 128, 0, st>>>(p, type, fn, rho_out, u_out);
     hook_end(hook, K_MACRO, st);
+}
+
+// One step of the reference's loop body (FluidCuda.cu:1277-1291), in place.
+template <class R, class S>
+void plain_launch_step(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *u, R *F, R *mv,
+                       const S *fc, S *fn, cudaStream_t st, LaunchHook *hook)
+{
+    plain_launch_step_split<R, S>(p, type, rho, mu, u, F, mv, fc, fn, rho, u, nullptr, st, hook);
 }
 
 template <class R, class S>
@@ -345,10 +363,11 @@ void plain_launch_wall(const KParams<R> &p, R *rho, cudaStream_t st)
     for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) k_wall_pass<R><<<gw, 128, 0, st>>>(p, s, rho, nullptr);
 }
 
-// mu and F without collision (diagnostic read-back of MU / FORCE).
+// mu and F without collision (diagnostic read-back of MU / FORCE); grad(mu)
+// into gm_out when it is non-null.
 template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
-                           cudaStream_t st)
+                           cudaStream_t st, R *gm_out)
 {
     const dim3 g = grid3(p, 128);
     if (p.wall_mode == 1) {
@@ -357,7 +376,7 @@ void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *
         for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) k_wall_pass<R><<<gw, 128, 0, st>>>(p, s, rho, mu);
     }
     k_chem_potential<R><<<g, 128, 0, st>>>(p, type, rho, mu);
-    k_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, F);
+    k_force<R><<<g, 128, 0, st>>>(p, type, rho, mu, F, gm_out);
 }
 
 }  // namespace cpmp

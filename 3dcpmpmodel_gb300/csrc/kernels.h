@@ -24,7 +24,13 @@ void plain_launch_macro(const KParams<R> &p, const uint8_t *type, const S *f, R 
                         cudaStream_t st);
 template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
-                           cudaStream_t st);
+                           cudaStream_t st, R *gm_out = nullptr);
+template <class R, class S>
+void plain_launch_step_split(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, const R *u, R *F, R *mv,
+                             const S *fc, S *fn, R *rho_out, R *u_out, R *gm_out, cudaStream_t st,
+                             LaunchHook *hook);
+extern template void plain_launch_step_split<float, float>(const KParams<float> &, const uint8_t *, float *, float *, const float *, float *, float *, const float *, float *, float *, float *, float *, cudaStream_t, LaunchHook *);
+extern template void plain_launch_step_split<double, double>(const KParams<double> &, const uint8_t *, double *, double *, const double *, double *, double *, const double *, double *, double *, double *, double *, cudaStream_t, LaunchHook *);
 
 template <class R>
 void plain_launch_wall(const KParams<R> &p, R *rho, cudaStream_t st);
@@ -33,11 +39,11 @@ extern template void plain_launch_wall<double>(const KParams<double> &, double *
 extern template void plain_launch_init<float, float>(const KParams<float> &, const DropletDev &, uint8_t *, float *, float *, float *, float *, cudaStream_t);
 extern template void plain_launch_step<float, float>(const KParams<float> &, const uint8_t *, float *, float *, float *, float *, float *, const float *, float *, cudaStream_t, LaunchHook *);
 extern template void plain_launch_macro<float, float>(const KParams<float> &, const uint8_t *, const float *, float *, float *, cudaStream_t);
-extern template void plain_launch_mu_force<float>(const KParams<float> &, const uint8_t *, float *, float *, float *, cudaStream_t);
+extern template void plain_launch_mu_force<float>(const KParams<float> &, const uint8_t *, float *, float *, float *, cudaStream_t, float *);
 extern template void plain_launch_init<double, double>(const KParams<double> &, const DropletDev &, uint8_t *, double *, double *, double *, double *, cudaStream_t);
 extern template void plain_launch_step<double, double>(const KParams<double> &, const uint8_t *, double *, double *, double *, double *, double *, const double *, double *, cudaStream_t, LaunchHook *);
 extern template void plain_launch_macro<double, double>(const KParams<double> &, const uint8_t *, const double *, double *, double *, cudaStream_t);
-extern template void plain_launch_mu_force<double>(const KParams<double> &, const uint8_t *, double *, double *, double *, cudaStream_t);
+extern template void plain_launch_mu_force<double>(const KParams<double> &, const uint8_t *, double *, double *, double *, cudaStream_t, double *);
 
 // ---- FUSED scheme (k_fused.cu) --------------------------------------------
 // storage: CPMP_STORE_F32 / F16 / BF16
@@ -83,23 +89,29 @@ void fused_launch_velocity(int storage, const KParams<float> &p, int P, const vo
                            const float *f0, const float *rho, float *u, cudaStream_t st);
 
 // ---- adjoint (k_adjoint_f32.cu, k_adjoint_f64.cu) ---------------------------
+// Four reals loaded or stored as one vector.
+template <class R>
+struct alignas(4 * sizeof(R)) Pack4 {
+    R x, y, z, w;
+};
 template <class R>
 struct AdjBufs {
     // dJ/df^n_q(x) = lamp_q(x) + lamrho(x) on fluid nodes, 0 on solid ones;
     // the *_next pair holds step n+1 while step n is being formed
-    R *lamp, *lamp_next, *lamrho, *lamrho_next, *lamF, *lammu;
+    R *lamp, *lamp_next, *lamrho, *lamrho_next, *lammu;
+    R *lamF;  // 4N: (dJ/dF_x, dJ/dF_y, dJ/dF_z, rho) per node
     double *ka_part, *gka, *gwall, *loss;
 };
 template <class R>
 void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, const double *target, AdjBufs<R> &b,
                      cudaStream_t st);
 template <class R>
-void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *mu, const R *F,
-                     AdjBufs<R> &b, cudaStream_t st);
+void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *gm, const R *F,
+                     AdjBufs<R> &b, cudaStream_t st, LaunchHook *hook);
 extern template void adj_launch_loss<float>(const KParams<float> &, const uint8_t *, const float *, const double *, AdjBufs<float> &, cudaStream_t);
-extern template void adj_launch_step<float>(const KParams<float> &, const uint8_t *, const float *, const float *, const float *, const float *, AdjBufs<float> &, cudaStream_t);
+extern template void adj_launch_step<float>(const KParams<float> &, const uint8_t *, const float *, const float *, const float *, const float *, AdjBufs<float> &, cudaStream_t, LaunchHook *);
 extern template void adj_launch_loss<double>(const KParams<double> &, const uint8_t *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
-extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
+extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t, LaunchHook *);
 
 // ---- diagnostics (k_diag.cu) ----------------------------------------------
 // Deterministic FP64 reduction: out[0] = sum rho (fluid), out[1] = max |mv|^2,

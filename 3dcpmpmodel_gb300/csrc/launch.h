@@ -17,13 +17,19 @@ enum KernelClass {
     K_MACRO = 4,    // density / velocity moments (MacroCalculate)
     K_FUSED = 5,    // fused mu + force + MRT + forcing + A-A stream
     K_DENSITY = 6,  // FUSED scheme density pass
-    K_CLASSES = 7
+    K_ADJ_COLLIDE = 7,  // adjoint: collision + streaming (R2)
+    K_ADJ_FORCE = 8,    // adjoint: non-ideal force (R3)
+    K_ADJ_MU = 9,       // adjoint: chemical potential + kappa partials (R4)
+    K_ADJ_WALL = 10,    // adjoint: wall layers + wall gradient (R5)
+    K_ADJ_SUM = 11,     // adjoint: loss and kappa reductions
+    K_CLASSES = 12
 };
 
 inline const char *kernel_class_name(int c)
 {
-    static const char *names[K_CLASSES] = {"wall",    "chem_potential", "force",  "collide_stream",
-                                           "macro",   "fused_collide",  "density"};
+    static const char *names[K_CLASSES] = {"wall",          "chem_potential", "force",       "collide_stream",
+                                           "macro",         "fused_collide",  "density",     "adj_collide",
+                                           "adj_force",     "adj_mu",         "adj_wall",    "adj_sum"};
     return (c >= 0 && c < K_CLASSES) ? names[c] : "?";
 }
 

@@ -58,6 +58,32 @@ def generate(src: str) -> None:
         f.write("\n".join(body) + "\n")
 
 
+def generate_gpu(src: str) -> None:
+    """Common_gpu.h: the reference's Common.h with its grid constants taken
+    from the macros REF_DX / REF_DY / REF_DZ (still compile-time constants,
+    as in the reference), for oracle/ref_gpu_bench.cu."""
+    os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(src, "Common.h"), encoding="latin-1") as f:
+        common = f.read().split("\n")
+    for ln, axis in ((25, "DY"), (26, "DX"), (27, "DZ")):
+        if not common[ln - 1].startswith(f"const int {axis}"):
+            raise RuntimeError(f"Common.h:{ln} is not the expected grid constant: {common[ln - 1]!r}")
+        common[ln - 1] = f"const int {axis} = REF_{axis};"
+    with open(os.path.join(OUT, "Common_gpu.h"), "w", encoding="latin-1") as f:
+        f.write("\n".join(common))
+
+
+def build_gpu_bench(dx: int, dy: int, dz: int) -> str:
+    """Compile oracle/ref_gpu_bench.cu for one grid (needs the generated
+    oracle/_ref/Common_gpu.h and ref_kernels.inc; nvcc for sm_103a)."""
+    out = os.path.join(OUT, f"ref_gpu_bench_{dx}x{dy}x{dz}")
+    cmd = ["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w",
+           f"-DREF_DX={dx}", f"-DREF_DY={dy}", f"-DREF_DZ={dz}", "-I", OUT,
+           os.path.join(HERE, "ref_gpu_bench.cu"), "-o", out]
+    subprocess.run(cmd, check=True)
+    return out
+
+
 def compile_lib() -> str:
     out = os.path.join(OUT, "libref.so")
     cmd = [
@@ -86,6 +112,7 @@ def build(src: str = DEFAULT_SRC) -> str | None:
     path, or None when neither the reference tree nor generated files exist."""
     if os.path.isfile(os.path.join(src, "FluidCuda.cu")):
         generate(src)
+        generate_gpu(src)
     if not (os.path.isfile(os.path.join(OUT, "Common_rt.h"))
             and os.path.isfile(os.path.join(OUT, "ref_kernels.inc"))):
         return None

@@ -48,7 +48,12 @@ def build_ref() -> str | None:
     spec = importlib.util.spec_from_file_location("cpmp_build_ref", os.path.join(HERE, "build_ref.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.build()
+    out = mod.build()
+    try:  # the reference's Tecplot writer, where the reference tree is present
+        mod.build_tecplot()
+    except Exception:
+        pass
+    return out
 
 
 def eos_constants(model: int, tr: float, a: float | None = None, b: float | None = None,
