@@ -75,7 +75,7 @@ struct cpmp_batch {
     KParams<float> *d_params = nullptr;
     BatchBox *d_boxes = nullptr;
     unsigned *d_counter = nullptr;
-    long long total_items = 0, nodes = 0, max_cols = 0, launches = 0;
+    long long total_items = 0, nodes = 0, max_cols = 0, max_pairs = 0, launches = 0;
     int max_dx = 0;
     cudaGraphExec_t gexec = nullptr;
     std::unique_ptr<LaunchHook> hook;
@@ -877,6 +877,7 @@ cpmp_status batch_upload(cpmp_batch *b)
     b->nodes = 0;
     b->max_dx = 0;
     b->max_cols = 0;
+    b->max_pairs = 0;
     for (int i = 0; i < nb; ++i) {
         cpmp_handle *h = b->boxes[i];
         kp[i] = make_kparams<float>(h);
@@ -893,6 +894,7 @@ cpmp_status batch_upload(cpmp_batch *b)
         b->nodes += h->n;
         b->max_dx = std::max(b->max_dx, h->p.dx);
         b->max_cols = std::max(b->max_cols, (long long)h->p.dx * h->p.dy);
+        b->max_pairs = std::max(b->max_pairs, (long long)h->p.dy * (h->p.dz / 2 + 1));
     }
     b->total_items = item;
     CK(cudaMemcpyAsync(b->d_params, kp.data(), nb * sizeof(KParams<float>), cudaMemcpyHostToDevice, b->st));
@@ -905,7 +907,7 @@ void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
 {
     const int P = (int)(b->boxes[0]->step & 1);
     fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params, b->d_boxes,
-                     (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, P, b->d_counter, b->st, hook);
+                     (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P, b->d_counter, b->st, hook);
     if (!bookkeeping) return;
     for (cpmp_handle *h : b->boxes) {
         h->step += 1;
@@ -931,11 +933,13 @@ extern "C" {
 cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch **out)
 {
     if (!params || !out || count < 1) return fail(CPMP_ERR_PARAM, "need count >= 1 parameter sets");
+    if (count > 65535) return fail(CPMP_ERR_PARAM, "at most 65535 boxes per batch");
     *out = nullptr;
     const cpmp_params &p0 = params[0];
     for (int i = 0; i < count; ++i) {
         const cpmp_params &p = params[i];
         if (p.scheme != CPMP_SCHEME_FUSED) return fail(CPMP_ERR_UNSUPPORTED, "batches run the FUSED scheme");
+        if (p.dx > 65535) return fail(CPMP_ERR_PARAM, "batch boxes have dx <= 65535");
         if (p.storage != p0.storage || p.lap_order != p0.lap_order || p.wall_mode != p0.wall_mode ||
             p.complex_bc != p0.complex_bc || p.device != p0.device)
             return fail(CPMP_ERR_PARAM, "boxes of a batch share storage, lap_order, wall_mode, complex_bc, device");
@@ -1029,7 +1033,7 @@ cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
             {
                 const int P = 1;
                 fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params,
-                                 b->d_boxes, (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, P,
+                                 b->d_boxes, (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P,
                                  b->d_counter, b->st, nullptr);
             }
             cudaError_t e = cudaStreamEndCapture(b->st, &g);
@@ -1275,7 +1279,8 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     ALLOC(b.lammu, n * sizeof(R), "lambda mu");
     ALLOC(b.lamrho, n * sizeof(R), "lambda rho");
     ALLOC(b.lamrho_next, n * sizeof(R), "lambda rho");
-    ALLOC(b.ka_part, nblocks * sizeof(double), "kappa partials");
+    ALLOC(b.ka_part, nblocks * sizeof(double), "loss partials");
+    ALLOC(b.ka_acc, nblocks * sizeof(double), "kappa partials");
     ALLOC(b.gka, sizeof(double), "kappa gradient");
     ALLOC(b.gwall, 2 * np * sizeof(double), "wall gradient");
     ALLOC(b.loss, sizeof(double), "loss");
@@ -1326,6 +1331,7 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
             return fail(CPMP_ERR_CUDA, std::string("adjoint sweep: ") + cudaGetErrorString(e));
         }
     }
+    adj_launch_finish<R>(kp, b, st);
     std::vector<double> gw(2 * np);
     double loss = 0, gka = 0;
     cudaMemcpyAsync(&loss, b.loss, sizeof(double), cudaMemcpyDeviceToHost, st);

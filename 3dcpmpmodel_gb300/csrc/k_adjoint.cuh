@@ -184,64 +184,107 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     for (int q = 0; q < Q; ++q) lamp[q * n + I] = fm[q] + R(cx(q)) * ajx + R(cy(q)) * ajy + R(cz(q)) * ajz;
 }
 
-// R3: force adjoint (stencil gathers of the packed (lamF, rho)).
+// R3: force adjoint.  A CTA owns an FT_Y x FT_Z column tile and marches
+// over FT_X planes of x; the packed (lamF, rho) of planes x-3 .. x+3 with a
+// halo of 3 in y and z sit in a seven-plane shared-memory ring, so every one
+// of the 54 stencil points of a node is one shared-memory vector load (each
+// global value is loaded once per CTA plus halo).  Periodic wrap in y and z
+// comes from per-CTA coordinate tables, in x from the plane index.
+constexpr int FT_Y = 4, FT_Z = 32, FT_X = 16;
+constexpr int FH_Y = FT_Y + 6, FH_Z = FT_Z + 6;
 template <class R>
-__global__ void __launch_bounds__(128, 4) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
-                                                      const Pack4<R> *lamF, R *lammu, R *lamrho)
+constexpr size_t adj_force_smem()
 {
-    NODE3D(p);
+    return sizeof(Pack4<R>) * 7 * FH_Y * FH_Z + sizeof(int) * (FH_Y + FH_Z);
+}
+template <class R>
+__global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
+                                                           const Pack4<R> *lamF, R *lammu, R *lamrho)
+{
+    extern __shared__ __align__(16) unsigned char fsm[];
+    Pack4<R> *ring = reinterpret_cast<Pack4<R> *>(fsm);
+    int *tabY = reinterpret_cast<int *>(ring + 7 * FH_Y * FH_Z);
+    int *tabZ = tabY + FH_Y;
+    constexpr int NT = FT_Y * FT_Z, PL = FH_Y * FH_Z;
+    const int z0 = blockIdx.x * FT_Z, y0 = blockIdx.y * FT_Y, x0 = blockIdx.z * FT_X;
+    const int x1 = min(x0 + FT_X, p.dx);
     const long long n = p.n;
-    const long long plane = (long long)p.dy * p.dz;
-    auto body = [&](auto nb) {
-        // for each lattice line (sx, sy, sz) with weight vector w (2 e on the
-        // axes, e on the diagonals): sum_d c_d (v(+d) - v(-d)) of v = w . lamF
-        // and of rho v; only the nonzero components of w enter
-        R sm = R(0), sr = R(0);
-        auto acc = [&](auto SX, auto SY, auto SZ) {
-            constexpr int sx = decltype(SX)::value, sy = decltype(SY)::value, sz = decltype(SZ)::value;
-            constexpr int axis = (sx != 0) + (sy != 0) + (sz != 0) == 1;
-            constexpr int wx = axis ? 2 * sx : sx, wy = axis ? 2 * sy : sy, wz = axis ? 2 * sz : sz;
-            auto lw = [&](const Pack4<R> &v4) -> R {
-                R v = R(0);
-                if constexpr (wx != 0) v += R(wx) * v4.x;
-                if constexpr (wy != 0) v += R(wy) * v4.y;
-                if constexpr (wz != 0) v += R(wz) * v4.z;
-                return v;
-            };
-#pragma unroll
-            for (int d = 1; d <= 3; ++d) {
-                const R cd = d == 1 ? R(45) : (d == 2 ? R(-9) : R(1));
-                const Pack4<R> vp = lamF[nb(sx * d, sy * d, sz * d)], vm = lamF[nb(-sx * d, -sy * d, -sz * d)];
-                const R lp = lw(vp), lm = lw(vm);
-                sm += cd * (vp.w * lp - vm.w * lm);
-                sr += cd * (lp - lm);
-            }
-        };
-        using P1 = std::integral_constant<int, 1>;
-        using Z0 = std::integral_constant<int, 0>;
-        using M1 = std::integral_constant<int, -1>;
-        acc(P1{}, Z0{}, Z0{});
-        acc(Z0{}, P1{}, Z0{});
-        acc(Z0{}, Z0{}, P1{});
-        acc(P1{}, P1{}, Z0{});
-        acc(P1{}, M1{}, Z0{});
-        acc(P1{}, Z0{}, P1{});
-        acc(P1{}, Z0{}, M1{});
-        acc(Z0{}, P1{}, P1{});
-        acc(Z0{}, P1{}, M1{});
-        lammu[I] = sm / R(360);
-        R add = -sr / R(360) / R(3);
-        if (type[I] == FLUID) {  // grad(mu) of the forward step, stored by its replay
-            const Pack4<R> l = lamF[I];
-            add -= l.x * gm[I] + l.y * gm[I + n] + l.z * gm[I + 2 * n];
+    for (int e = threadIdx.x; e < FH_Y + FH_Z; e += NT) {
+        if (e < FH_Y) tabY[e] = wrap_off(y0 - 3 + e, p.dy);
+        else tabZ[e - FH_Y] = wrap_off(z0 - 3 + (e - FH_Y), p.dz);
+    }
+    __syncthreads();
+    auto slot = [](int x) { return ((x % 7) + 7) % 7; };
+    auto load = [&](int x) {
+        const long long base = (long long)wrap_off(x, p.dx) * p.dy;
+        Pack4<R> *dst = ring + slot(x) * PL;
+        for (int e = threadIdx.x; e < PL; e += NT) {
+            const int ly = e / FH_Z, lz = e - ly * FH_Z;
+            dst[e] = lamF[(base + tabY[ly]) * p.dz + tabZ[lz]];
         }
-        lamrho[I] += add;
     };
-    if (interior_node(p, i, j, k, 3)) body(Nb<true, R>{p, i, j, k, I, plane});
-    else body(Nb<false, R>{p, i, j, k, I, plane});
+    for (int x = x0 - 3; x < x0 + 3; ++x) load(x);
+    const int tz = threadIdx.x % FT_Z, ty = threadIdx.x / FT_Z;
+    const int j = y0 + ty, k = z0 + tz;
+    const bool active = j < p.dy && k < p.dz;
+    const int c = (ty + 3) * FH_Z + (tz + 3);
+    for (int x = x0; x < x1; ++x) {
+        load(x + 3);
+        __syncthreads();
+        if (active) {
+            const long long I = ((long long)x * p.dy + j) * p.dz + k;
+            // for each lattice line (sx, sy, sz) with weight vector w (2 e on
+            // the axes, e on the diagonals): sum_d c_d (v(+d) - v(-d)) of
+            // v = w . lamF and of rho v; only the nonzero components of w enter
+            R sm = R(0), sr = R(0);
+            auto acc = [&](auto SX, auto SY, auto SZ) {
+                constexpr int sx = decltype(SX)::value, sy = decltype(SY)::value, sz = decltype(SZ)::value;
+                constexpr int axis = (sx != 0) + (sy != 0) + (sz != 0) == 1;
+                constexpr int wx = axis ? 2 * sx : sx, wy = axis ? 2 * sy : sy, wz = axis ? 2 * sz : sz;
+                auto lw = [&](const Pack4<R> &v4) -> R {
+                    R v = R(0);
+                    if constexpr (wx != 0) v += R(wx) * v4.x;
+                    if constexpr (wy != 0) v += R(wy) * v4.y;
+                    if constexpr (wz != 0) v += R(wz) * v4.z;
+                    return v;
+                };
+#pragma unroll
+                for (int d = 1; d <= 3; ++d) {
+                    const R cd = d == 1 ? R(45) : (d == 2 ? R(-9) : R(1));
+                    const int o = sy * d * FH_Z + sz * d;
+                    const Pack4<R> vp = ring[slot(x + sx * d) * PL + c + o];
+                    const Pack4<R> vm = ring[slot(x - sx * d) * PL + c - o];
+                    const R lp = lw(vp), lm = lw(vm);
+                    sm += cd * (vp.w * lp - vm.w * lm);
+                    sr += cd * (lp - lm);
+                }
+            };
+            using P1 = std::integral_constant<int, 1>;
+            using Z0 = std::integral_constant<int, 0>;
+            using M1 = std::integral_constant<int, -1>;
+            acc(P1{}, Z0{}, Z0{});
+            acc(Z0{}, P1{}, Z0{});
+            acc(Z0{}, Z0{}, P1{});
+            acc(P1{}, P1{}, Z0{});
+            acc(P1{}, M1{}, Z0{});
+            acc(P1{}, Z0{}, P1{});
+            acc(P1{}, Z0{}, M1{});
+            acc(Z0{}, P1{}, P1{});
+            acc(Z0{}, P1{}, M1{});
+            lammu[I] = sm / R(360);
+            R add = -sr / R(360) / R(3);
+            if (type[I] == FLUID) {  // grad(mu) of the forward step, stored by its replay
+                const Pack4<R> l = ring[slot(x) * PL + c];
+                add -= l.x * gm[I] + l.y * gm[I + n] + l.z * gm[I + 2 * n];
+            }
+            lamrho[I] += add;
+        }
+        __syncthreads();  // plane x-3's slot is refilled with x+4 next
+    }
 }
 
-// R4: chemical-potential adjoint; per-block FP64 partials of dJ/dka.
+// R4: chemical-potential adjoint; per-block FP64 partials of dJ/dka, added
+// to the block's running sum (fixed order, so the result is deterministic).
 template <class R>
 __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *type, const R *rho, const R *lammu,
                                                 R *lamrho, double *ka_part)
@@ -293,8 +336,8 @@ __global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *typ
         if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0)
-        ka_part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = red[0];
+    if (threadIdx.x == 0)  // per-block sums over all steps; added up once at the end
+        ka_part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] += red[0];
 }
 
 // R5: wall adjoint in one launch.  The forward sets layer 2 = E(layer 3),
@@ -414,6 +457,15 @@ void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, con
     const dim3 g = grid3(p, 128);
     k_adj_loss<R><<<g, 128, 0, st>>>(p, type, rho, target, b.lamp_next, b.lamrho_next, b.ka_part);
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.loss, 0);
+    cudaMemsetAsync(b.ka_acc, 0, sizeof(double) * g.x * g.y * g.z, st);
+}
+
+// dJ/dka: the per-block sums of every reverse step, added up in fixed order.
+template <class R>
+void adj_launch_finish(const KParams<R> &p, AdjBufs<R> &b, cudaStream_t st)
+{
+    const dim3 g = grid3(p, 128);
+    k_adj_sum<<<1, 256, 0, st>>>(b.ka_acc, (long long)g.x * g.y * g.z, b.gka, 0);
 }
 
 // One reverse step.  rho/u/gm/F hold the forward intermediates of step n
@@ -429,15 +481,25 @@ void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, con
     hook_begin(hook, K_ADJ_COLLIDE, st);
     k_adj_collide<R><<<g, 128, 0, st>>>(p, type, rho, u, F, b.lamp_next, b.lamrho_next, b.lamp, lamF, b.lamrho);
     hook_end(hook, K_ADJ_COLLIDE, st);
-    hook_begin(hook, K_ADJ_FORCE, st);
-    k_adj_force<R><<<g, 128, 0, st>>>(p, type, gm, lamF, b.lammu, b.lamrho);
-    hook_end(hook, K_ADJ_FORCE, st);
+    {
+        // shared-memory opt-in (FP64 needs more than 48 KB), once per device
+        static int attr_dev = -1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev != attr_dev) {
+            cudaFuncSetAttribute(k_adj_force<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)adj_force_smem<R>());
+            attr_dev = dev;
+        }
+        const dim3 gf((unsigned)((p.dz + FT_Z - 1) / FT_Z), (unsigned)((p.dy + FT_Y - 1) / FT_Y),
+                      (unsigned)((p.dx + FT_X - 1) / FT_X));
+        hook_begin(hook, K_ADJ_FORCE, st);
+        k_adj_force<R><<<gf, FT_Y * FT_Z, adj_force_smem<R>(), st>>>(p, type, gm, lamF, b.lammu, b.lamrho);
+        hook_end(hook, K_ADJ_FORCE, st);
+    }
     hook_begin(hook, K_ADJ_MU, st);
-    k_adj_mu<R><<<g, 128, 0, st>>>(p, type, rho, b.lammu, b.lamrho, b.ka_part);
+    k_adj_mu<R><<<g, 128, 0, st>>>(p, type, rho, b.lammu, b.lamrho, b.ka_acc);
     hook_end(hook, K_ADJ_MU, st);
-    hook_begin(hook, K_ADJ_SUM, st);
-    k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.gka, 1);
-    hook_end(hook, K_ADJ_SUM, st);
     if (p.wall_mode == 1) {
         const dim3 gw((unsigned)((p.dx + WT - 1) / WT), (unsigned)((p.dy + WT - 1) / WT), 2);
         hook_begin(hook, K_ADJ_WALL, st);

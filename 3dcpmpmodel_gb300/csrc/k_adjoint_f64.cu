@@ -4,4 +4,5 @@
 namespace cpmp {
 template void adj_launch_loss<double>(const KParams<double> &, const uint8_t *, const double *, const double *, AdjBufs<double> &, cudaStream_t);
 template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t, LaunchHook *);
+template void adj_launch_finish<double>(const KParams<double> &, AdjBufs<double> &, cudaStream_t);
 }  // namespace cpmp

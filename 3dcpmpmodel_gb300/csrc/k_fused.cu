@@ -290,7 +290,8 @@ void batch_collide_l(const FusedTile &t, const KParams<float> *params, const Bat
 
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, int P, unsigned *counter, cudaStream_t st, LaunchHook *hook)
+                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter, cudaStream_t st,
+                      LaunchHook *hook)
 {
     if (wall_mode == 1) {
         const dim3 gw((unsigned)((max_cols + 127) / 128), (unsigned)nbox);
@@ -313,7 +314,8 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density_batch<S><<<dim3((unsigned)max_dx, (unsigned)nbox), 256, 0, st>>>(params, boxes, 1 - P);
+        const dim3 gd((unsigned)((max_pairs + 127) / 128), (unsigned)max_dx, (unsigned)nbox);
+        k_density_batch<S><<<gd, 128, 0, st>>>(params, boxes, 1 - P);
     });
     hook_end(hook, K_DENSITY, st);
 }

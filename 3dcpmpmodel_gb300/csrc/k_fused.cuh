@@ -611,26 +611,22 @@ __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
     }
 }
 
-// Batched density pass: one block per (box, x plane), threads over the
-// plane's node pairs (the pairing of k_density).
+// Batched density pass, one node pair per thread (the pairing of
+// k_density): blockIdx.z is the box, blockIdx.y the x plane, blockIdx.x the
+// plane's pairs in blocks of 128; blocks past a box's extent exit at once.
 template <class S>
-__global__ void __launch_bounds__(256) k_density_batch(const KParams<float> *__restrict__ params,
+__global__ void __launch_bounds__(128) k_density_batch(const KParams<float> *__restrict__ params,
                                                        const BatchBox *__restrict__ boxes, int P)
 {
-    const int b = blockIdx.y;
+    const int b = blockIdx.z, i = blockIdx.y;
     const KParams<float> &p = params[b];
-    const int i = blockIdx.x;
     if (i >= p.dx) return;
-    const BatchBox &bx = boxes[b];
-    const S *h = (const S *)bx.h;
-    const float *f0 = bx.f0[P];
-    float *rho = bx.rho[P];
     const int per_col = pairs_per_column(p.dz);
-    const int nplane = p.dy * per_col;
-    for (int e = threadIdx.x; e < nplane; e += blockDim.x) {
-        const int j = e / per_col, t = e - j * per_col;
-        density_pair<S>(p, P, h, f0, rho, i, j, pair_k0(p, i, j, t));
-    }
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.dy * per_col) return;
+    const BatchBox &bx = boxes[b];
+    const int j = e / per_col, t = e - j * per_col;
+    density_pair<S>(p, P, (const S *)bx.h, bx.f0[P], bx.rho[P], i, j, pair_k0(p, i, j, t));
 }
 
 template <class S, int TY, int TZ, int L>

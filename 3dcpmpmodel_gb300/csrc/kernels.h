@@ -74,10 +74,12 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 // fused collide over all (box, tile, chunk) work items, the batched density
 // pass.  params/boxes are device arrays of nbox entries; counter is one
 // device unsigned (reset here); max_dx / max_cols bound the boxes' x extent
-// and wall columns.
+// and wall columns, max_pairs the density pass's node pairs per x plane
+// (dy * (dz / 2 + 1)).
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, int P, unsigned *counter, cudaStream_t st, LaunchHook *hook);
+                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter, cudaStream_t st,
+                      LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).
 void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,
@@ -100,11 +102,17 @@ struct AdjBufs {
     // the *_next pair holds step n+1 while step n is being formed
     R *lamp, *lamp_next, *lamrho, *lamrho_next, *lammu;
     R *lamF;  // 4N: (dJ/dF_x, dJ/dF_y, dJ/dF_z, rho) per node
-    double *ka_part, *gka, *gwall, *loss;
+    double *ka_part;  // per-block partials of one reduction
+    double *ka_acc;   // per-block dJ/dka sums over all reverse steps
+    double *gka, *gwall, *loss;
 };
 template <class R>
 void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, const double *target, AdjBufs<R> &b,
                      cudaStream_t st);
+template <class R>
+void adj_launch_finish(const KParams<R> &p, AdjBufs<R> &b, cudaStream_t st);
+extern template void adj_launch_finish<float>(const KParams<float> &, AdjBufs<float> &, cudaStream_t);
+extern template void adj_launch_finish<double>(const KParams<double> &, AdjBufs<double> &, cudaStream_t);
 template <class R>
 void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, const R *u, const R *gm, const R *F,
                      AdjBufs<R> &b, cudaStream_t st, LaunchHook *hook);

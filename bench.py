@@ -46,6 +46,11 @@ WORKLOADS = {
     # reference's CUDA step is timed on this GPU as well
     "c3ref": dict(name="reference_defaults_480cube_prw", dx=480, dy=480, dz=480, model=202, tr=0.7,
                   radius=100.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8),
+    # the reference's own defaults (CP-PRW, T/Tc 0.7) on the largest cube its
+    # 32-bit population index allows (19 N < 2^31): the grid on which the
+    # reference's CUDA step is timed on this GPU as well
+    "c3ref": dict(name="reference_defaults_480cube_prw", dx=480, dy=480, dz=480, model=202, tr=0.7,
+                  radius=100.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8),
     "c1": dict(name="periodic_64cube_cs", dx=64, dy=64, dz=64, model=206, tr=0.85, eos_a=0.5,
                eos_b=4.0, radius=16.0, width=2.0, wall_mode=0, base_pt=0.0, k=0.2, ka=0.01,
                tau=1.0, centre=(32.0, 32.0, 32.0)),
