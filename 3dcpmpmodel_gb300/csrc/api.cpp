@@ -106,7 +106,10 @@ KParams<R> make_kparams(const cpmp_handle *h)
     k.ka = (R)h->p.ka;
     k.k1 = (R)h->p.k1;
     k.k2 = (R)h->p.k2;
-    for (int q = 0; q < CPMP_Q; ++q) k.ts[q] = (R)h->ts[q];
+    for (int q = 0; q < CPMP_Q; ++q) {
+        k.ts[q] = (R)h->ts[q];
+        k.omts[q] = (R)(1.0 - h->ts[q]);
+    }
     k.wall = (const R *)h->wall;
     return k;
 }

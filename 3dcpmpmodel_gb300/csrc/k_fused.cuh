@@ -176,16 +176,17 @@ __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
 template <class S, int P, bool EVEN>
 __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const S *__restrict__ h,
                                                   const float *__restrict__ f0, float *__restrict__ rho,
-                                                  long long I)
+                                                  unsigned I)
 {
-    const long long n = p.n;
-    const long long plane = (long long)p.dy * p.dz;
+    // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
+    const unsigned n = (unsigned)p.n;
+    const int plane = p.dy * p.dz;
     float2 hv[Q - 1], a[Q - 1];
 #pragma unroll
     for (int q = 1; q < Q; ++q) {
-        const long long off = cx(q) * plane + cy(q) * (long long)p.dz + cz(q);
-        const long long src = I - off;
-        const long long hi = P == 0 ? (long long)(q - 1) * n + I : (long long)(opp(q) - 1) * n + src;
+        const int off = cx(q) * plane + cy(q) * p.dz + cz(q);
+        const unsigned src = I - (unsigned)off;
+        const size_t hi = P == 0 ? (size_t)n * (unsigned)(q - 1) + I : (size_t)n * (unsigned)(opp(q) - 1) + src;
         const bool odd_off = (cz(q) & 1) != 0;
         hv[q - 1] = load_pair<S>(h + hi, EVEN && (P == 0 || !odd_off));
         a[q - 1] = load_pair<float>(f0 + src, EVEN && !odd_off);
@@ -216,7 +217,7 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
         if (in1) density_node<S>(p, P, h, f0, rho, i, j, k0 + 1);
         return;
     }
-    const long long I = ((long long)i * p.dy + j) * p.dz + k0;
+    const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
     if ((p.dz & 1) == 0) {
         if (P == 0) density_pair_fast<S, 0, true>(p, h, f0, rho, I);
         else density_pair_fast<S, 1, true>(p, h, f0, rho, I);
@@ -248,7 +249,6 @@ __global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const 
 }
 
 // --------------------------------------------------------- fused step ----
-__device__ __forceinline__ int ring_slot(int x, int nr) { return ((x % nr) + nr) % nr; }
 __device__ __forceinline__ int wrap_small(int a, int n)
 {
     while (a < 0) a += n;
@@ -260,11 +260,14 @@ template <int TY, int TZ, int L>
 struct FusedGeom {
     static constexpr int RH = 3 + L;                 // rho halo (y, z)
     static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
-    static constexpr int NR = 2 * L + 2;             // rho planes x+3-L .. x+4+L (one prefetched)
+    // ring sizes are powers of two so a plane's slot is (x & (size - 1)),
+    // also for the negative x of the prologue
+    static constexpr int NR = 8;                     // rho planes x+3-L .. x+4+L (one prefetched)
+    static_assert(2 * L + 2 <= NR, "rho ring too small");
     static constexpr int MY = TY + 6, MZ = TZ + 6;   // (rho, mu) pairs, halo 3, planes x-3..x+3
     static constexpr int AY = TY + 2, AZ = TZ + 2;   // rest populations, halo 1, planes x-1..x+2
     static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
-    static constexpr int RM_PAIRS = 7 * MY * MZ;
+    static constexpr int RM_PAIRS = 8 * MY * MZ;     // (rho, mu) planes x-3 .. x+3 (+1 being written)
     static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
     static constexpr int TAB_INTS = 2 * RY + RZ;
     static constexpr size_t BASE_BYTES = sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
@@ -283,11 +286,6 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-__device__ __forceinline__ int mod_small(int t, int m)
-{
-    return t < 0 ? t + m : (t >= m ? t - m : t);
-}
 
 // One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
 // x.  Shared-memory rings:
@@ -341,7 +339,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
 
     auto issue_rho = [&](int xlog) {
         const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
-        float *dst = srho + ring_slot(xlog, NR) * (RY * RZ);
+        float *dst = srho + (xlog & (NR - 1)) * (RY * RZ);
         for (int e = threadIdx.x; e < RY * RZ; e += NT) {
             const int ly = e / RZ, lz = e - ly * RZ;
             cp_async4(dst + e, src + (unsigned)(tabYdz[ly] + tabZ[lz]));
@@ -349,7 +347,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
     };
     auto issue_f0 = [&](int xlog) {
         const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
-        float *dst = sf0 + ring_slot(xlog, 4) * (AY * AZ);
+        float *dst = sf0 + (xlog & 3) * (AY * AZ);
         for (int e = threadIdx.x; e < AY * AZ; e += NT) {
             const int ly = e / AZ, lz = e - ly * AZ;
             cp_async4(dst + e, src + (unsigned)(tabYdz[ly + RH - 1] + tabZ[lz + RH - 1]));
@@ -357,14 +355,12 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
     };
     auto comp_mu = [&](int xlog) {
         const int gx = wrap_small(xlog, p.dx);
-        float2 *dst = srm + ring_slot(xlog, 7) * (MY * MZ);
-        const float *rc = srho + ring_slot(xlog, NR) * (RY * RZ);
-        const float *rm1 = srho + ring_slot(xlog - 1, NR) * (RY * RZ);
-        const float *rp1 = srho + ring_slot(xlog + 1, NR) * (RY * RZ);
-        const float *rm2 = srho + ring_slot(xlog - 2, NR) * (RY * RZ);
-        const float *rp2 = srho + ring_slot(xlog + 2, NR) * (RY * RZ);
-        const float *rm3 = L == 3 ? srho + ring_slot(xlog - 3, NR) * (RY * RZ) : rc;
-        const float *rp3 = L == 3 ? srho + ring_slot(xlog + 3, NR) * (RY * RZ) : rc;
+        float2 *dst = srm + (xlog & 7) * (MY * MZ);
+        auto rpl = [&](int xx) -> const float * { return srho + (xx & (NR - 1)) * (RY * RZ); };
+        const float *rc = rpl(xlog), *rm1 = rpl(xlog - 1), *rp1 = rpl(xlog + 1);
+        const float *rm2 = rpl(xlog - 2), *rp2 = rpl(xlog + 2);
+        const float *rm3 = L == 3 ? rpl(xlog - 3) : rc;
+        const float *rp3 = L == 3 ? rpl(xlog + 3) : rc;
         for (int e = threadIdx.x; e < MY * MZ; e += NT) {
             const int my = e / MZ, mz = e - my * MZ;
             const int c = (my + L) * RZ + (mz + L);
@@ -459,10 +455,10 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
         __syncthreads();
         if (active) {
             // force from the (rho, mu) ring
-            const int s7 = ring_slot(x, 7);
+
             const float2 *pl[7];
 #pragma unroll
-            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + mod_small(s7 + d, 7) * (MY * MZ);
+            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + ((x + d) & 7) * (MY * MZ);
             // (rho, mu) pairs: each first difference is one paired add and one
             // paired fma per stencil distance (Blackwell FADD2 / FFMA2)
             float2 g0 = make_float2(0.f, 0.f), g1 = g0, g2 = g0;  // (grad rho, grad mu) per axis
@@ -497,11 +493,11 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             const float Fz = -gm[2] * r + gr[2] * (1.0f / 3.0f);
 
             // decode with the sources' rest populations as anchors
-            const int s4 = ring_slot(x, 4);
+
             const float *fa[3];
-            fa[0] = sf0 + mod_small(s4 - 1, 4) * (AY * AZ);  // plane x-1
-            fa[1] = sf0 + s4 * (AY * AZ);                    // plane x
-            fa[2] = sf0 + mod_small(s4 + 1, 4) * (AY * AZ);  // plane x+1
+            fa[0] = sf0 + ((x - 1) & 3) * (AY * AZ);  // plane x-1
+            fa[1] = sf0 + (x & 3) * (AY * AZ);        // plane x
+            fa[2] = sf0 + ((x + 1) & 3) * (AY * AZ);  // plane x+1
             const float a0 = fa[1][ac];
             float f[Q];
             f[0] = a0;
@@ -526,9 +522,9 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
                 qp[13] = -p.k1 * gr[0] * gr[1];
                 qp[14] = -p.k1 * gr[2] * gr[1];
                 qp[15] = -p.k1 * gr[0] * gr[2];
-                collide_mrt_edm<float>(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, qp);
+                collide_mrt_edm_fused(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, qp);
             } else {
-                collide_mrt_edm<float>(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, nullptr);
+                collide_mrt_edm_fused(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, nullptr);
             }
 
             // encode against this node's new rest population and stream

@@ -53,6 +53,7 @@ struct KParams {
     R kk;              // K^2
     R A, B, T, ka, k1, k2;
     R ts[Q];
+    R omts[Q];         // 1 - ts, rounded once on the host
     const R *wall;     // [2][dx*dy] wall chemical potential, bottom then top
 };
 
@@ -280,6 +281,27 @@ __device__ __forceinline__ void collide_mrt_edm(R f[Q], R rho, R ux, R uy, R uz,
         m[a] = v;
     }
     inverse_moments<R>(m, f);
+}
+
+// The same collision for the FUSED kernel with the relaxation written as
+// m* = (1 - s) (m - meq(u)) + meq(u + F/rho): two operations per moment
+// instead of four (mathematically the reference's update; rounding differs).
+__device__ __forceinline__ void collide_mrt_edm_fused(float f[Q], float rho, float ux, float uy, float uz,
+                                                      float Fx, float Fy, float Fz, const float ts[Q],
+                                                      const float omts[Q], const float *qp)
+{
+    float m[Q], me[Q], me1[Q];
+    moments<float>(f, m);
+    meq_moments<float>(rho, ux, uy, uz, me);
+    const float ir = 1.0f / rho;
+    meq_moments<float>(rho, ux + Fx * ir, uy + Fy * ir, uz + Fz * ir, me1);
+#pragma unroll
+    for (int a = 0; a < Q; ++a) {
+        float v = a >= 16 ? omts[a] * m[a] : fmaf(omts[a], m[a] - me[a], me1[a]);  // meq = 0 for 16..18
+        if (qp) v = fmaf(qp[a], ts[a], v);
+        m[a] = v;
+    }
+    inverse_moments<float>(m, f);
 }
 
 }  // namespace cpmp
