@@ -18,9 +18,9 @@ import numpy as np
 
 from . import _abi
 from ._abi import (CPMP_F32, CPMP_F64, FIELD, MODEL, SCHEME, STORE, WALL, CpmpError,
-                   Diag, Droplet, Params, lib)
+                   Diag, Droplet, Impact, Params, lib)
 
-__all__ = ["Solver", "Batch", "Params", "Droplet", "Diag", "CpmpError", "lib", "default_params",
+__all__ = ["Solver", "Batch", "Params", "Droplet", "Diag", "Impact", "CpmpError", "lib", "default_params",
            "coexistence", "MODEL", "SCHEME", "STORE", "WALL", "FIELD", "reference_ts"]
 
 Q = 19
@@ -179,6 +179,13 @@ class Solver:
         code = CPMP_F64 if a.dtype == np.float64 else CPMP_F32
         _abi.check(self._lib.cpmp_set_field(self._h, FIELD[field], code,
                                             a.ctypes.data_as(C.c_void_p), C.c_size_t(a.nbytes)))
+
+    def impact(self) -> dict:
+        """Droplet-impact sums of the current state (ComputeEnergy,
+        Computetangential_velocity, SaveSpreadtime), on the device."""
+        d = Impact()
+        _abi.check(self._lib.cpmp_impact_diag(self._h, C.byref(d)))
+        return {k: getattr(d, k) for k, _ in Impact._fields_}
 
     def reduce(self, allow_nonfinite: bool = False) -> dict:
         """CalcMacroCPU + ContactAngle(0, DY/2) + the Laplace probe, on the device."""

@@ -59,6 +59,12 @@ class Diag(C.Structure):
                 ("step", C.c_longlong)]
 
 
+class Impact(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("v", "v_xy", "v_z", "mv", "mv_xy", "mv_z", "energy", "energy_xy",
+                                           "energy_z", "tangential", "m_tangential", "drop_momentum",
+                                           "drop_mass", "drop_velocity")]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "cpmp_params_default": (None, [C.c_void_p]),
@@ -72,6 +78,7 @@ SIGNATURES = {
     "cpmp_get_field": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
     "cpmp_set_field": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
     "cpmp_reduce": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "cpmp_impact_diag": (C.c_int, [C.c_void_p, C.c_void_p]),
     "cpmp_get_eos": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_double)] * 6),
     "cpmp_coexistence": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                    C.c_char_p] + [C.POINTER(C.c_double)] * 6),

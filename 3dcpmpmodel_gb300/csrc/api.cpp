@@ -55,6 +55,7 @@ struct cpmp_handle {
     float *f0[2] = {nullptr, nullptr};
     void *wall = nullptr;
     double *partials = nullptr, *dout = nullptr;
+    double *impact_partials = nullptr;  // allocated by the first cpmp_impact_diag
     long long step = 0;
     bool initialised = false;
     std::unique_ptr<LaunchHook> hook;
@@ -119,13 +120,13 @@ void free_all(cpmp_handle *h)
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
     void *ptrs[] = {h->type, h->rho, h->rho2, h->mu, h->u, h->mv, h->F, h->fb[0], h->fb[1], h->h, h->f0[0], h->f0[1],
-                    h->wall, h->partials, h->dout};
+                    h->wall, h->partials, h->dout, h->impact_partials};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     h->type = nullptr;
     h->rho = h->rho2 = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
     h->f0[0] = h->f0[1] = nullptr;
-    h->partials = h->dout = nullptr;
+    h->partials = h->dout = h->impact_partials = nullptr;
     if (h->st) cudaStreamDestroy(h->st);
     h->st = nullptr;
 }
@@ -721,6 +722,51 @@ cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
     return CPMP_OK;
 }
 
+cpmp_status cpmp_impact_diag(cpmp_handle *h, cpmp_impact *out)
+{
+    if (!h || !out) return fail(CPMP_ERR_PARAM, "null argument");
+    CK(cudaSetDevice(h->p.device));
+    std::memset(out, 0, sizeof(*out));
+    if (!h->plain) {
+        cpmp_status s = fused_diag_fields(h);
+        if (s != CPMP_OK) return s;
+    }
+    const int nq = diag_impact_quantities();
+    if (!h->impact_partials) {
+        const size_t bytes = (size_t)nq * diag_partial_blocks(h->n) * sizeof(double) + 16 * sizeof(double);
+        cpmp_status s = dalloc((void **)&h->impact_partials, bytes, "impact partials");
+        if (s != CPMP_OK) return s;
+    }
+    double *dres = h->impact_partials + (size_t)nq * diag_partial_blocks(h->n);
+    const double mid = (h->den_g + h->den_l) / 2;
+    if (h->f64)
+        diag_launch_impact<double>(h->type, (const double *)h->rho, (const double *)h->mv, h->p.dx, h->p.dy, h->p.dz,
+                                   mid, h->impact_partials, dres, h->st);
+    else
+        diag_launch_impact<float>(h->type, (const float *)h->rho, (const float *)h->mv, h->p.dx, h->p.dy, h->p.dz,
+                                  mid, h->impact_partials, dres, h->st);
+    h->launches += 2;
+    double r[16] = {0};
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(r, dres, nq * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    out->v = r[0];
+    out->v_xy = r[1];
+    out->v_z = r[2];
+    out->mv = r[3];
+    out->mv_xy = r[4];
+    out->mv_z = r[5];
+    out->energy = r[6];
+    out->energy_xy = r[7];
+    out->energy_z = r[8];
+    out->tangential = r[9];
+    out->m_tangential = r[10];
+    out->drop_momentum = r[11];
+    out->drop_mass = r[12];
+    out->drop_velocity = r[12] > 0 ? r[11] / r[12] : 0.0;
+    return CPMP_OK;
+}
+
 cpmp_status cpmp_get_eos(cpmp_handle *h, double *den_g, double *den_l, double *A, double *B, double *T, double *Rc)
 {
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
@@ -1280,10 +1326,11 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     ALLOC(b.lamp_next, 19 * n * sizeof(R), "lambda partial");
     ALLOC(b.lamF, 4 * n * sizeof(R), "lambda F");
     ALLOC(b.lammu, n * sizeof(R), "lambda mu");
+    ALLOC(b.lmr, 2 * n * sizeof(R), "lambda mu (fluid), rho");
     ALLOC(b.lamrho, n * sizeof(R), "lambda rho");
     ALLOC(b.lamrho_next, n * sizeof(R), "lambda rho");
     ALLOC(b.ka_part, nblocks * sizeof(double), "loss partials");
-    ALLOC(b.ka_acc, nblocks * sizeof(double), "kappa partials");
+    ALLOC(b.ka_acc, (size_t)adj_tiled_blocks(h->p.dx, h->p.dy, h->p.dz) * sizeof(double), "kappa partials");
     ALLOC(b.gka, sizeof(double), "kappa gradient");
     ALLOC(b.gwall, 2 * np * sizeof(double), "wall gradient");
     ALLOC(b.loss, sizeof(double), "loss");

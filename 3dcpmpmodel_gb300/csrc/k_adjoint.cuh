@@ -130,16 +130,24 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     // back into slot opp(q) of this node
     R ls[Q];
     const R lr_here = lamrho_next[I];
-    auto gather = [&](auto nb) {
+    auto gather = [&](auto nb, auto CHECK) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const long long D = nb(cx(q), cy(q), cz(q));
-            ls[q] = type[D] == FLUID ? lamp_next[q * n + D] + lamrho_next[D] : lamp_next[opp(q) * n + I] + lr_here;
+            const bool dfl = decltype(CHECK)::value ? type[D] == FLUID : true;
+            ls[q] = dfl ? lamp_next[q * n + D] + lamrho_next[D] : lamp_next[opp(q) * n + I] + lr_here;
         }
     };
     const long long plane = (long long)p.dy * p.dz;
-    if (interior_node(p, i, j, k, 1)) gather(Nb<true, R>{p, i, j, k, I, plane});
-    else gather(Nb<false, R>{p, i, j, k, I, plane});
+    // node tags are the wall layers alone, so a node at least two layers
+    // from the walls has fluid neighbours only
+    const bool no_wall = p.wall_mode == 0 || (k >= 4 && k <= p.dz - 5);
+    if (interior_node(p, i, j, k, 1) && no_wall)
+        gather(Nb<true, R>{p, i, j, k, I, plane}, std::false_type{});
+    else if (interior_node(p, i, j, k, 1))
+        gather(Nb<true, R>{p, i, j, k, I, plane}, std::true_type{});
+    else
+        gather(Nb<false, R>{p, i, j, k, I, plane}, std::true_type{});
     // mu* = M^-T lambda* = diag(1/norm) M lambda*
     R ms[Q];
     moments<R>(ls, ms);
@@ -186,24 +194,30 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
 
 // R3: force adjoint.  A CTA owns an FT_Y x FT_Z column tile and marches
 // over FT_X planes of x; the packed (lamF, rho) of planes x-3 .. x+3 with a
-// halo of 3 in y and z sit in a seven-plane shared-memory ring, so every one
-// of the 54 stencil points of a node is one shared-memory vector load (each
-// global value is loaded once per CTA plus halo).  Periodic wrap in y and z
-// comes from per-CTA coordinate tables, in x from the plane index.
+// halo of 3 in y and z sit in an eight-plane shared-memory ring (plane x+4 is
+// copied in with cp.async while plane x is computed), so every one of the 54
+// stencil points of a node is one shared-memory vector load and each global
+// value is loaded once per CTA plus halo.  Periodic wrap in y and z comes from
+// per-CTA coordinate tables, in x from the plane index.
 constexpr int FT_Y = 4, FT_Z = 32, FT_X = 16;
 constexpr int FH_Y = FT_Y + 6, FH_Z = FT_Z + 6;
+// CTAs of the tiled R3 / R4 launches
+__host__ __device__ constexpr long long adj_mu_blocks(int dx, int dy, int dz)
+{
+    return (long long)((dz + FT_Z - 1) / FT_Z) * ((dy + FT_Y - 1) / FT_Y) * ((dx + FT_X - 1) / FT_X);
+}
 template <class R>
 constexpr size_t adj_force_smem()
 {
-    return sizeof(Pack4<R>) * 7 * FH_Y * FH_Z + sizeof(int) * (FH_Y + FH_Z);
+    return sizeof(Pack4<R>) * 8 * FH_Y * FH_Z + sizeof(int) * (FH_Y + FH_Z);
 }
 template <class R>
 __global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
-                                                           const Pack4<R> *lamF, R *lammu, R *lamrho)
+                                                           const Pack4<R> *lamF, R *lammu, Pack2<R> *lmr, R *lamrho)
 {
     extern __shared__ __align__(16) unsigned char fsm[];
     Pack4<R> *ring = reinterpret_cast<Pack4<R> *>(fsm);
-    int *tabY = reinterpret_cast<int *>(ring + 7 * FH_Y * FH_Z);
+    int *tabY = reinterpret_cast<int *>(ring + 8 * FH_Y * FH_Z);
     int *tabZ = tabY + FH_Y;
     constexpr int NT = FT_Y * FT_Z, PL = FH_Y * FH_Z;
     const int z0 = blockIdx.x * FT_Z, y0 = blockIdx.y * FT_Y, x0 = blockIdx.z * FT_X;
@@ -214,22 +228,32 @@ __global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const ui
         else tabZ[e - FH_Y] = wrap_off(z0 - 3 + (e - FH_Y), p.dz);
     }
     __syncthreads();
-    auto slot = [](int x) { return ((x % 7) + 7) % 7; };
+    auto slot = [](int x) { return x & 7; };
     auto load = [&](int x) {
         const long long base = (long long)wrap_off(x, p.dx) * p.dy;
         Pack4<R> *dst = ring + slot(x) * PL;
         for (int e = threadIdx.x; e < PL; e += NT) {
             const int ly = e / FH_Z, lz = e - ly * FH_Z;
-            dst[e] = lamF[(base + tabY[ly]) * p.dz + tabZ[lz]];
+            const Pack4<R> *src = lamF + (base + tabY[ly]) * p.dz + tabZ[lz];
+#pragma unroll
+            for (int b = 0; b < (int)sizeof(Pack4<R>); b += 16) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(reinterpret_cast<char *>(dst + e) + b);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                             "l"(reinterpret_cast<const char *>(src) + b)
+                             : "memory");
+            }
         }
     };
-    for (int x = x0 - 3; x < x0 + 3; ++x) load(x);
+    for (int x = x0 - 3; x <= x0 + 3; ++x) load(x);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     const int tz = threadIdx.x % FT_Z, ty = threadIdx.x / FT_Z;
     const int j = y0 + ty, k = z0 + tz;
     const bool active = j < p.dy && k < p.dz;
     const int c = (ty + 3) * FH_Z + (tz + 3);
     for (int x = x0; x < x1; ++x) {
-        load(x + 3);
+        load(x + 4);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // planes up to x+3 have landed
         __syncthreads();
         if (active) {
             const long long I = ((long long)x * p.dy + j) * p.dz + k;
@@ -271,73 +295,126 @@ __global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const ui
             acc(P1{}, Z0{}, M1{});
             acc(Z0{}, P1{}, P1{});
             acc(Z0{}, P1{}, M1{});
-            lammu[I] = sm / R(360);
+            const R lmu = sm / R(360);
+            const bool fl = type[I] == FLUID;
+            const Pack4<R> own = ring[slot(x) * PL + c];
+            lammu[I] = lmu;
+            lmr[I] = Pack2<R>{fl ? lmu : R(0), own.w};  // lam_mu on fluid nodes and rho, for R4
             R add = -sr / R(360) / R(3);
-            if (type[I] == FLUID) {  // grad(mu) of the forward step, stored by its replay
-                const Pack4<R> l = ring[slot(x) * PL + c];
-                add -= l.x * gm[I] + l.y * gm[I + n] + l.z * gm[I + 2 * n];
+            if (fl)  // grad(mu) of the forward step, stored by its replay
+                add -= own.x * gm[I] + own.y * gm[I + n] + own.z * gm[I + 2 * n];
+            lamrho[I] += add;
+        }
+        __syncthreads();  // plane x-3's slot is refilled with x+5 next
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// R4: chemical-potential adjoint, tiled like R3: an eight-plane ring of the
+// packed (lam_mu on fluid nodes, rho) with halo 3 (cp.async one plane
+// ahead); the Laplacians of both are read from shared memory.  Each CTA adds
+// its FP64 partial of dJ/dka to its own running sum (fixed order, so the
+// result is deterministic).
+template <class R>
+constexpr size_t adj_mu_smem()
+{
+    return sizeof(Pack2<R>) * 8 * FH_Y * FH_Z + sizeof(int) * (FH_Y + FH_Z);
+}
+template <class R>
+__global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_mu(KParams<R> p, const uint8_t *type, const Pack2<R> *lmr,
+                                                        R *lamrho, double *ka_part)
+{
+    extern __shared__ __align__(16) unsigned char msm[];
+    Pack2<R> *ring = reinterpret_cast<Pack2<R> *>(msm);
+    int *tabY = reinterpret_cast<int *>(ring + 8 * FH_Y * FH_Z);
+    int *tabZ = tabY + FH_Y;
+    __shared__ double red[FT_Y * FT_Z / 32];
+    constexpr int NT = FT_Y * FT_Z, PL = FH_Y * FH_Z;
+    const int z0 = blockIdx.x * FT_Z, y0 = blockIdx.y * FT_Y, x0 = blockIdx.z * FT_X;
+    const int x1 = min(x0 + FT_X, p.dx);
+    for (int e = threadIdx.x; e < FH_Y + FH_Z; e += NT) {
+        if (e < FH_Y) tabY[e] = wrap_off(y0 - 3 + e, p.dy);
+        else tabZ[e - FH_Y] = wrap_off(z0 - 3 + (e - FH_Y), p.dz);
+    }
+    __syncthreads();
+    auto load = [&](int x) {
+        const long long base = (long long)wrap_off(x, p.dx) * p.dy;
+        Pack2<R> *dst = ring + (x & 7) * PL;
+        for (int e = threadIdx.x; e < PL; e += NT) {
+            const int ly = e / FH_Z, lz = e - ly * FH_Z;
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + e);
+            const Pack2<R> *src = lmr + (base + tabY[ly]) * p.dz + tabZ[lz];
+            if (sizeof(Pack2<R>) == 8)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(src) : "memory");
+            else
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+        }
+    };
+    for (int x = x0 - 3; x <= x0 + 3; ++x) load(x);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    const int tz = threadIdx.x % FT_Z, ty = threadIdx.x / FT_Z;
+    const int j = y0 + ty, k = z0 + tz;
+    const bool active = j < p.dy && k < p.dz;
+    const int c = (ty + 3) * FH_Z + (tz + 3);
+    double gka = 0.0;
+    for (int x = x0; x < x1; ++x) {
+        load(x + 4);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // planes up to x+3 have landed
+        __syncthreads();
+        if (active) {
+            const long long I = ((long long)x * p.dy + j) * p.dz + k;
+            // the two Laplacians (the stencil is symmetric, so the adjoint's
+            // is the forward's): .x = lam_mu restricted to fluid, .y = rho
+            auto at = [&](int a, int b, int cc) -> const Pack2<R> & {
+                return ring[((x + a) & 7) * PL + c + b * FH_Z + cc];
+            };
+            R lx, ly;
+            if (p.lap_order == 7) {
+                const Pack2<R> &o = at(0, 0, 0);
+                lx = -o.x * R(1470);
+                ly = -o.y * R(1470);
+#pragma unroll
+                for (int d = 1; d <= 3; ++d) {
+                    const R w = d == 1 ? R(270) : (d == 2 ? R(-27) : R(2));
+                    const Pack2<R> &a1 = at(d, 0, 0), &a2 = at(-d, 0, 0), &a3 = at(0, d, 0), &a4 = at(0, -d, 0),
+                                   &a5 = at(0, 0, d), &a6 = at(0, 0, -d);
+                    lx += w * (a1.x + a2.x + a3.x + a4.x + a5.x + a6.x);
+                    ly += w * (a1.y + a2.y + a3.y + a4.y + a5.y + a6.y);
+                }
+                lx /= R(180);
+                ly /= R(180);
+            } else {
+                auto l5 = [&](auto f) -> R {
+                    return (-f(0, 0, 0) * R(90) + (-f(-2, 0, 0) + f(-1, 0, 0) * R(16) + f(1, 0, 0) * R(16) - f(2, 0, 0)) +
+                            (-f(0, -2, 0) + f(0, -1, 0) * R(16) + f(0, 1, 0) * R(16) - f(0, 2, 0)) +
+                            (-f(0, 0, -2) + f(0, 0, -1) * R(16) + f(0, 0, 1) * R(16) - f(0, 0, 2))) /
+                           R(12);
+                };
+                lx = l5([&](int a, int b, int cc) { return at(a, b, cc).x; });
+                ly = l5([&](int a, int b, int cc) { return at(a, b, cc).y; });
+            }
+            R add = -p.ka * lx;
+            if (type[I] == FLUID) {
+                const Pack2<R> &o = at(0, 0, 0);
+                add += p.kk * dmu0<R>(p.eos, p.A, p.B, p.T, o.y) * o.x;
+                gka += -(double)o.x * (double)ly;
             }
             lamrho[I] += add;
         }
-        __syncthreads();  // plane x-3's slot is refilled with x+4 next
+        __syncthreads();  // plane x-3's slot is refilled with x+5 next
     }
-}
-
-// R4: chemical-potential adjoint; per-block FP64 partials of dJ/dka, added
-// to the block's running sum (fixed order, so the result is deterministic).
-template <class R>
-__global__ void __launch_bounds__(128) k_adj_mu(KParams<R> p, const uint8_t *type, const R *rho, const R *lammu,
-                                                R *lamrho, double *ka_part)
-{
-    __shared__ double red[128];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, i = blockIdx.z;
-    double gka = 0.0;
-    if (k < p.dz) {
-        const long long I = ((long long)i * p.dy + j) * p.dz + k;
-        const long long plane = (long long)p.dy * p.dz;
-        auto body = [&](auto nb) {
-            // Laplacian of lam_mu restricted to fluid nodes (the stencil is
-            // symmetric), and the forward's Laplacian of rho for dJ/dka
-            auto lm = [&](int a, int b, int c) -> R {
-                const long long J = nb(a, b, c);
-                return type[J] == FLUID ? lammu[J] : R(0);
-            };
-            auto rr = [&](int a, int b, int c) -> R { return rho[nb(a, b, c)]; };
-            auto lap = [&](auto f) -> R {
-                if (p.lap_order == 7) {
-                    R s7 = -f(0, 0, 0) * R(1470);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // warp shuffles, then the warp sums in order (deterministic)
 #pragma unroll
-                    for (int d = 1; d <= 3; ++d) {
-                        const R w = d == 1 ? R(270) : (d == 2 ? R(-27) : R(2));
-                        s7 += w * (f(d, 0, 0) + f(-d, 0, 0) + f(0, d, 0) + f(0, -d, 0) + f(0, 0, d) + f(0, 0, -d));
-                    }
-                    return s7 / R(180);
-                }
-                return (-f(0, 0, 0) * R(90) + (-f(-2, 0, 0) + f(-1, 0, 0) * R(16) + f(1, 0, 0) * R(16) - f(2, 0, 0)) +
-                        (-f(0, -2, 0) + f(0, -1, 0) * R(16) + f(0, 1, 0) * R(16) - f(0, 2, 0)) +
-                        (-f(0, 0, -2) + f(0, 0, -1) * R(16) + f(0, 0, 1) * R(16) - f(0, 0, 2))) /
-                       R(12);
-            };
-            R add = -p.ka * lap(lm);
-            if (type[I] == FLUID) {
-                const R r = rho[I];
-                add += p.kk * dmu0<R>(p.eos, p.A, p.B, p.T, r) * lammu[I];
-                gka = -(double)lammu[I] * (double)lap(rr);
-            }
-            lamrho[I] += add;
-        };
-        if (interior_node(p, i, j, k, 3)) body(Nb<true, R>{p, i, j, k, I, plane});
-        else body(Nb<false, R>{p, i, j, k, I, plane});
-    }
-    red[threadIdx.x] = gka;
+    for (int o = 16; o > 0; o >>= 1) gka += __shfl_down_sync(0xffffffffu, gka, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = gka;
     __syncthreads();
-    for (int o = 64; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < NT / 32; ++w) t += red[w];
+        ka_part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] += t;
     }
-    if (threadIdx.x == 0)  // per-block sums over all steps; added up once at the end
-        ka_part[((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] += red[0];
 }
 
 // R5: wall adjoint in one launch.  The forward sets layer 2 = E(layer 3),
@@ -457,7 +534,7 @@ void adj_launch_loss(const KParams<R> &p, const uint8_t *type, const R *rho, con
     const dim3 g = grid3(p, 128);
     k_adj_loss<R><<<g, 128, 0, st>>>(p, type, rho, target, b.lamp_next, b.lamrho_next, b.ka_part);
     k_adj_sum<<<1, 256, 0, st>>>(b.ka_part, (long long)g.x * g.y * g.z, b.loss, 0);
-    cudaMemsetAsync(b.ka_acc, 0, sizeof(double) * g.x * g.y * g.z, st);
+    cudaMemsetAsync(b.ka_acc, 0, sizeof(double) * adj_mu_blocks(p.dx, p.dy, p.dz), st);
 }
 
 // dJ/dka: the per-block sums of every reverse step, added up in fixed order.
@@ -465,7 +542,7 @@ template <class R>
 void adj_launch_finish(const KParams<R> &p, AdjBufs<R> &b, cudaStream_t st)
 {
     const dim3 g = grid3(p, 128);
-    k_adj_sum<<<1, 256, 0, st>>>(b.ka_acc, (long long)g.x * g.y * g.z, b.gka, 0);
+    k_adj_sum<<<1, 256, 0, st>>>(b.ka_acc, adj_mu_blocks(p.dx, p.dy, p.dz), b.gka, 0);
 }
 
 // One reverse step.  rho/u/gm/F hold the forward intermediates of step n
@@ -489,17 +566,18 @@ void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, con
         if (dev != attr_dev) {
             cudaFuncSetAttribute(k_adj_force<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)adj_force_smem<R>());
+            cudaFuncSetAttribute(k_adj_mu<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_mu_smem<R>());
             attr_dev = dev;
         }
         const dim3 gf((unsigned)((p.dz + FT_Z - 1) / FT_Z), (unsigned)((p.dy + FT_Y - 1) / FT_Y),
                       (unsigned)((p.dx + FT_X - 1) / FT_X));
         hook_begin(hook, K_ADJ_FORCE, st);
-        k_adj_force<R><<<gf, FT_Y * FT_Z, adj_force_smem<R>(), st>>>(p, type, gm, lamF, b.lammu, b.lamrho);
+        k_adj_force<R><<<gf, FT_Y * FT_Z, adj_force_smem<R>(), st>>>(p, type, gm, lamF, b.lammu, b.lmr, b.lamrho);
         hook_end(hook, K_ADJ_FORCE, st);
+        hook_begin(hook, K_ADJ_MU, st);
+        k_adj_mu<R><<<gf, FT_Y * FT_Z, adj_mu_smem<R>(), st>>>(p, type, b.lmr, b.lamrho, b.ka_acc);
+        hook_end(hook, K_ADJ_MU, st);
     }
-    hook_begin(hook, K_ADJ_MU, st);
-    k_adj_mu<R><<<g, 128, 0, st>>>(p, type, rho, b.lammu, b.lamrho, b.ka_acc);
-    hook_end(hook, K_ADJ_MU, st);
     if (p.wall_mode == 1) {
         const dim3 gw((unsigned)((p.dx + WT - 1) / WT), (unsigned)((p.dy + WT - 1) / WT), 2);
         hook_begin(hook, K_ADJ_WALL, st);

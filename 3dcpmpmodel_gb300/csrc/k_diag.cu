@@ -131,6 +131,89 @@ __global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__rest
     }
 }
 
+// ------------------------------------------------ droplet-impact sums ----
+// ComputeEnergy (FluidCuda.cu:737-787) and Computetangential_velocity
+// (:790-898): over fluid nodes with rho > mid in 2 <= i < DX-2,
+// 2 <= j < DY-2, 2 <= k < DZ-2 -- sum |MV|, |MV_xy|, MVz, the same weighted
+// by rho, the kinetic energies rho |MV|^2 / 2 (all, xy, z), and the
+// velocity along the azimuth about (DX/2, DY/2) and its rho-weighted sum;
+// SaveSpreadtime (:1128-1150): over every node with rho > mid and
+// 2 <= k < DZ-2, the sums of rho |MV| and rho.  Per-block FP64 partials in a
+// fixed order, then a fixed-order sum per quantity.
+constexpr int kImpactQ = 13;
+template <class R>
+__global__ void __launch_bounds__(kRedThreads) k_impact_partial(const uint8_t *__restrict__ type,
+                                                               const R *__restrict__ rho,
+                                                               const R *__restrict__ mv, int dx, int dy, int dz,
+                                                               double mid, double *__restrict__ part)
+{
+    const double PI = 3.14159265358979323846264338327950288;
+    const long long n = (long long)dx * dy * dz;
+    double acc[kImpactQ];
+#pragma unroll
+    for (int q = 0; q < kImpactQ; ++q) acc[q] = 0.0;
+    for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
+         I += (long long)gridDim.x * blockDim.x) {
+        const double d = (double)rho[I];
+        if (!(d > mid)) continue;
+        const int k = (int)(I % dz), j = (int)((I / dz) % dy), i = (int)(I / ((long long)dz * dy));
+        if (k < 2 || k >= dz - 2) continue;
+        const double a = (double)mv[I], b = (double)mv[I + n], c = (double)mv[I + 2 * n];
+        const double s2 = a * a + b * b, s3 = s2 + c * c;
+        acc[11] += d * sqrt(s3);
+        acc[12] += d;
+        if (type[I] != FLUID || i < 2 || i >= dx - 2 || j < 2 || j >= dy - 2) continue;
+        const double v3 = sqrt(s3), v2 = sqrt(s2);
+        acc[0] += v3;
+        acc[1] += v2;
+        acc[2] += c;
+        acc[3] += d * v3;
+        acc[4] += d * v2;
+        acc[5] += d * c;
+        acc[6] += d * s3 / 2;
+        acc[7] += d * s2 / 2;
+        acc[8] += d * (c * c) / 2;
+        double al = atan2((double)(j - dy / 2), (double)(i - dx / 2)) / PI * 180;
+        if (al < 0) al = al + 360;
+        al = al / 180 * PI;
+        const double t = a * sin(al) + b * cos(al);
+        acc[9] += t;
+        acc[10] += t * d;
+    }
+    __shared__ double sw[kRedThreads / 32][kImpactQ];
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < kImpactQ; ++q) {
+        const double v = warp_sum(acc[q]);
+        if (l == 0) sw[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kImpactQ) {
+        double v = 0.0;
+        for (int ww = 0; ww < kRedThreads / 32; ++ww) v += sw[ww][threadIdx.x];
+        part[(long long)blockIdx.x * kImpactQ + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_impact_final(const double *__restrict__ part, int nb, double *__restrict__ out)
+{
+    const int q = threadIdx.x;
+    if (q >= kImpactQ) return;
+    double v = 0.0;
+    for (int b = 0; b < nb; ++b) v += part[(long long)b * kImpactQ + q];
+    out[q] = v;
+}
+
+template <class R>
+void diag_launch_impact(const uint8_t *type, const R *rho, const R *mv, int dx, int dy, int dz, double mid,
+                        double *partials, double *out, cudaStream_t st)
+{
+    const int nb = diag_partial_blocks((long long)dx * dy * dz);
+    k_impact_partial<R><<<nb, kRedThreads, 0, st>>>(type, rho, mv, dx, dy, dz, mid, partials);
+    k_impact_final<<<1, 32, 0, st>>>(partials, nb, out);
+}
+int diag_impact_quantities() { return kImpactQ; }
+
 template <class R>
 void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long n, double *partials,
                       double *out, cudaStream_t st)
@@ -397,5 +480,7 @@ template void diag_launch_contact_angle<float>(const float *, int, int, int, int
 template void diag_launch_contact_angle<double>(const double *, int, int, int, int, double, double, double *, cudaStream_t);
 template void diag_launch_laplace<float>(const float *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
 template void diag_launch_laplace<double>(const double *, int, int, int, int, double, double, double, double, double *, cudaStream_t);
+template void diag_launch_impact<float>(const uint8_t *, const float *, const float *, int, int, int, double, double *, double *, cudaStream_t);
+template void diag_launch_impact<double>(const uint8_t *, const double *, const double *, int, int, int, double, double *, double *, cudaStream_t);
 
 }  // namespace cpmp

@@ -97,10 +97,18 @@ struct alignas(4 * sizeof(R)) Pack4 {
     R x, y, z, w;
 };
 template <class R>
+struct alignas(2 * sizeof(R)) Pack2 {
+    R x, y;
+};
+// CTAs of the adjoint's tiled force and chemical-potential launches (the
+// length of AdjBufs::ka_acc).
+long long adj_tiled_blocks(int dx, int dy, int dz);
+template <class R>
 struct AdjBufs {
     // dJ/df^n_q(x) = lamp_q(x) + lamrho(x) on fluid nodes, 0 on solid ones;
     // the *_next pair holds step n+1 while step n is being formed
     R *lamp, *lamp_next, *lamrho, *lamrho_next, *lammu;
+    Pack2<R> *lmr;  // (lammu on fluid nodes, 0 on solid ones; rho) per node
     R *lamF;  // 4N: (dJ/dF_x, dJ/dF_y, dJ/dF_z, rho) per node
     double *ka_part;  // per-block partials of one reduction
     double *ka_acc;   // per-block dJ/dka sums over all reverse steps
@@ -142,6 +150,15 @@ void diag_launch_laplace(const R *rho, int dx, int dy, int dz, int eos, double A
 void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const float *F, float *mv,
                     long long n, cudaStream_t st);
 
+// Droplet-impact sums (ComputeEnergy, Computetangential_velocity,
+// SaveSpreadtime): out[13] in the order of cpmp_impact; `partials` holds
+// diag_impact_quantities() * diag_partial_blocks(n) doubles.
+int diag_impact_quantities();
+template <class R>
+void diag_launch_impact(const uint8_t *type, const R *rho, const R *mv, int dx, int dy, int dz, double mid,
+                        double *partials, double *out, cudaStream_t st);
+extern template void diag_launch_impact<float>(const uint8_t *, const float *, const float *, int, int, int, double, double *, double *, cudaStream_t);
+extern template void diag_launch_impact<double>(const uint8_t *, const double *, const double *, int, int, int, double, double *, double *, cudaStream_t);
 extern template void diag_launch_mass<float>(const uint8_t *, const float *, const float *, long long, double *, double *, cudaStream_t);
 extern template void diag_launch_mass<double>(const uint8_t *, const double *, const double *, long long, double *, double *, cudaStream_t);
 extern template void diag_launch_contact_angle<float>(const float *, int, int, int, int, double, double, double *, cudaStream_t);

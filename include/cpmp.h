@@ -177,6 +177,23 @@ cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *
  * on which the reference stops (FluidCuda.cu:1632-1646). */
 cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out);
 
+/* Droplet-impact diagnostics (FP64 device sums, deterministic order).
+ * "Liquid" means rho > (rho_g + rho_l)/2; MV is the physical velocity. */
+typedef struct cpmp_impact {
+    /* ComputeEnergy (FluidCuda.cu:737-787): fluid liquid nodes with
+     * 2 <= i < DX-2, 2 <= j < DY-2, 2 <= k < DZ-2 */
+    double v, v_xy, v_z;            /* sum |MV|, |MV_xy|, MV_z */
+    double mv, mv_xy, mv_z;         /* the same weighted by rho */
+    double energy, energy_xy, energy_z; /* sum rho |MV|^2 / 2, xy part, z part */
+    /* Computetangential_velocity (FluidCuda.cu:790-898): same nodes; the
+     * velocity along the azimuth about (DX/2, DY/2), and weighted by rho */
+    double tangential, m_tangential;
+    /* SaveSpreadtime (FluidCuda.cu:1128-1150): every liquid node with
+     * 2 <= k < DZ-2; drop_velocity = drop_momentum / drop_mass */
+    double drop_momentum, drop_mass, drop_velocity;
+} cpmp_impact;
+cpmp_status cpmp_impact_diag(cpmp_handle *h, cpmp_impact *out);
+
 /* Coexistence densities (lattice units) the handle resolved, and the EOS
  * constants it derived (SetMultiphase, FluidCuda.cu:1318-1384). */
 cpmp_status cpmp_get_eos(cpmp_handle *h, double *den_g, double *den_l, double *A, double *B,

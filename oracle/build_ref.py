@@ -7,6 +7,8 @@ TEST INFRASTRUCTURE ONLY.  Generates, into oracle/_ref/ (git-ignored):
   declarations (Common.h:25-27 and :33-34); everything else is verbatim.
 * ``ref_kernels.inc``: FluidCuda.cu lines 115-116 (the GridIndex/LineIndex
   launch-index macros) and 188-463 (the kernels), verbatim.
+* ``ref_impact.inc``: FluidCuda.cu lines 737-783 and 786-898 (the host
+  diagnostics ComputeEnergy and Computetangential_velocity), verbatim.
 
 and compiles ``oracle/ref_shim.cpp`` against them into ``oracle/_ref/libref.so``.
 
@@ -32,6 +34,8 @@ GRID_LINES = {  # Common.h line (1-based) -> expected declaration prefix
     34: "const int DXY",
 }
 INDEX_FIRST, INDEX_LAST = 115, 116
+# host diagnostics ComputeEnergy and Computetangential_velocity
+IMPACT_RANGES = ((737, 783, "void ComputeEnergy()"), (786, 898, "void Computetangential_velocity()"))
 KERNEL_FIRST, KERNEL_LAST = 188, 463
 
 
@@ -56,6 +60,14 @@ def generate(src: str) -> None:
     body = ["#ifndef GridIndex"] + index + ["#endif"] + body
     with open(os.path.join(OUT, "ref_kernels.inc"), "w", encoding="latin-1") as f:
         f.write("\n".join(body) + "\n")
+    impact = []
+    for first, last, head in IMPACT_RANGES:
+        part = lines[first - 1:last]
+        if head not in part[0]:
+            raise RuntimeError(f"FluidCuda.cu:{first} is not {head}")
+        impact += part
+    with open(os.path.join(OUT, "ref_impact.inc"), "w", encoding="latin-1") as f:
+        f.write("\n".join(impact) + "\n")
 
 
 def generate_gpu(src: str) -> None:

@@ -574,3 +574,62 @@ void orc_contact_angle(const orc_params *p, const double *dens, int tier, double
 #undef T
     out[0] = cl; out[1] = cr; out[2] = cap; out[3] = xl; out[4] = xr; out[5] = H; out[6] = L;
 }
+
+/* Droplet-impact sums, FP64, sequential in the reference's loop order.
+ * ComputeEnergy (FluidCuda.cu:737-787) and Computetangential_velocity
+ * (:790-898): fluid nodes with rho > mid, 2 <= i < DX-2, 2 <= j < DY-2,
+ * 2 <= k < DZ-2, loops i, j, k.  SaveSpreadtime (:1128-1150): every node with
+ * rho > mid and 2 <= k < DZ-2, loops i, j, k.
+ * out = {V, VXY, VZ, MV, MVXY, MVZ, energy, energyXY, energyZ,
+ *        tangential_vel, Mtangential_vel, mvel, dropmass} */
+void orc_impact(const orc_params *p, const uint8_t *type, const double *dens, const double *mvx,
+                const double *mvy, const double *mvz, double den_g, double den_l, double out[13])
+{
+    const int DX = p->dx, DY = p->dy, DZ = p->dz;
+    const double PI2 = 3.14159265358979323846264338327950288;
+    const double mid = (den_g + den_l) / 2;
+    double s[11] = {0};
+    for (int i = 2; i < DX - 2; i++)
+        for (int j = 2; j < DY - 2; j++)
+            for (int k = 2; k < DZ - 2; k++) {
+                const long I = IDX(p, i, j, k);
+                if (type[I] == FLUID && dens[I] > mid) {
+                    const double a = mvx[I], b = mvy[I], c = mvz[I], d = dens[I];
+                    s[0] += sqrt(a * a + b * b + c * c);
+                    s[1] += sqrt(a * a + b * b);
+                    s[2] += c;
+                    s[3] += d * sqrt(a * a + b * b + c * c);
+                    s[4] += d * sqrt(a * a + b * b);
+                    s[5] += d * c;
+                    s[6] += d * (a * a + b * b + c * c) / 2;
+                    s[7] += d * (a * a + b * b) / 2;
+                    s[8] += d * (c * c) / 2;
+                }
+            }
+    for (int i = 2; i < DX - 2; i++)
+        for (int j = 2; j < DY - 2; j++)
+            for (int k = 2; k < DZ - 2; k++) {
+                const long I = IDX(p, i, j, k);
+                if (type[I] == FLUID && dens[I] > mid) {
+                    double alpha = atan2((double)(j - DY / 2), (double)(i - DX / 2)) / PI2 * 180;
+                    if (alpha < 0) alpha = alpha + 360;
+                    alpha = alpha / 180 * PI2;
+                    const double t = mvx[I] * sin(alpha) + mvy[I] * cos(alpha);
+                    s[9] += t;
+                    s[10] += t * dens[I];
+                }
+            }
+    double mvel = 0, mass = 0;
+    for (int i = 0; i < DX; i++)
+        for (int j = 0; j < DY; j++)
+            for (int k = 2; k < DZ - 2; k++) {
+                const long I = IDX(p, i, j, k);
+                if (dens[I] > mid) {
+                    mvel += dens[I] * sqrt(mvx[I] * mvx[I] + mvy[I] * mvy[I] + mvz[I] * mvz[I]);
+                    mass += dens[I];
+                }
+            }
+    for (int q = 0; q < 11; ++q) out[q] = s[q];
+    out[11] = mvel;
+    out[12] = mass;
+}

@@ -195,6 +195,10 @@ class Setup:
         return self.dx * self.dy * self.dz
 
 
+IMPACT_KEYS = ("v", "v_xy", "v_z", "mv", "mv_xy", "mv_z", "energy", "energy_xy", "energy_z", "tangential",
+               "m_tangential", "drop_momentum", "drop_mass")
+
+
 class State:
     """Fields of one run in the reference layout, advanced by a CPU backend."""
 
@@ -302,6 +306,15 @@ class State:
         self.lib.orc_contact_angle(C.byref(self.p), self._ptr(self.dens), C.c_int(t),
                                    C.c_double(self.den_g), C.c_double(self.den_l), out)
         return dict(zip(("ca_left", "ca_right", "ca_cap", "x_left", "x_right", "h", "l"), list(out)))
+
+    def impact(self):
+        """Droplet-impact sums (ComputeEnergy, Computetangential_velocity,
+        SaveSpreadtime): dict in the order of cpmp_impact."""
+        out = (C.c_double * 13)()
+        self.lib.orc_impact(C.byref(self.p), self._ptr(self.type), self._ptr(self.dens), self._ptr(self.mvx),
+                            self._ptr(self.mvy), self._ptr(self.mvz), C.c_double(self.den_g),
+                            C.c_double(self.den_l), out)
+        return dict(zip(IMPACT_KEYS, list(out)))
 
     def view(self, a):
         return a.reshape(self.s.dx, self.s.dy, self.s.dz)

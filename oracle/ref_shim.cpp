@@ -68,6 +68,21 @@ namespace v7c {
 #undef COMPLEXCHEMBOUNDARY
 }  // namespace v7c
 
+// The reference's host droplet-impact diagnostics (FluidCuda.cu:737-898)
+// over the reference's globals of the same names (FluidCuda.cu:52-66); they
+// append their sums to text files under data/ of the working directory.
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+namespace rh {
+using namespace std;
+char *Type;
+double *Dens, *MVx, *MVy, *MVz;
+double DenG, DenL, BasePt, Radius, Diameter, Tau, DropVy, DimTime;
+int NowStep;
+#include "ref_impact.inc"
+}  // namespace rh
+
 namespace {
 
 template <class F>
@@ -168,6 +183,24 @@ int ref_step(int variant, int nsteps, char *type, double *dens, double *pote, do
         }
     }
     return 0;
+}
+
+// Runs ComputeEnergy and Computetangential_velocity once for step `nowstep`
+// (1 writes the files' header lines first, as the reference does).
+void ref_impact(char *type, double *dens, double *mvx, double *mvy, double *mvz, double den_g, double den_l,
+                double base_pt, int nowstep)
+{
+    rh::Type = type;
+    rh::Dens = dens;
+    rh::MVx = mvx;
+    rh::MVy = mvy;
+    rh::MVz = mvz;
+    rh::DenG = den_g;
+    rh::DenL = den_l;
+    rh::BasePt = base_pt;
+    rh::NowStep = nowstep;
+    rh::ComputeEnergy();
+    rh::Computetangential_velocity();
 }
 
 }  // extern "C"

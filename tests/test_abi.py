@@ -41,9 +41,9 @@ def test_struct_layout_matches_header(cpmp):
 #include <stddef.h>
 #include "cpmp.h"
 int main(void){
- printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(cpmp_params), offsetof(cpmp_params, ts),
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(cpmp_params), offsetof(cpmp_params, ts),
         offsetof(cpmp_params, cocurve_dir), offsetof(cpmp_params, device), sizeof(cpmp_droplet),
-        sizeof(cpmp_diag), offsetof(cpmp_diag, step));
+        sizeof(cpmp_diag), offsetof(cpmp_diag, step), sizeof(cpmp_impact), offsetof(cpmp_impact, drop_velocity));
  return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -54,7 +54,7 @@ int main(void){
         vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True).stdout.split()]
     P, D, G = cpmp.Params, cpmp.Droplet, cpmp.Diag
     assert vals == [C.sizeof(P), P.ts.offset, P.cocurve_dir.offset, P.device.offset, C.sizeof(D),
-                    C.sizeof(G), G.step.offset]
+                    C.sizeof(G), G.step.offset, C.sizeof(cpmp.Impact), cpmp.Impact.drop_velocity.offset]
 
 
 def test_defaults_are_the_reference_initialize(cpmp):
