@@ -28,7 +28,7 @@ UNITS = [
     ("tecplot.cpp", []),
     ("k_plain_f32.cu", []),
     ("k_plain_f64.cu", ["--fmad=false"]),
-    ("k_fused.cu", []),
+    ("k_fused.cu", ["--fmad=false"]),
     ("k_diag.cu", []),
     ("k_adjoint_f32.cu", []),
     ("k_adjoint_f64.cu", ["--fmad=false"]),

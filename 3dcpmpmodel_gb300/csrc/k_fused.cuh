@@ -560,7 +560,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
 
 // One box: CTA (bx, by, bz) owns z tile bx, y tile by and x chunk bz.
 template <class S, int TY, int TZ, int L>
-__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
+__global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
     k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
                     float *__restrict__ f0n, const float *__restrict__ rho, int xl)
 {
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
 // x chunk) work items from an atomic counter until none are left.  Uneven
 // box sizes balance themselves; every box shares the tile shape and march.
 template <class S, int TY, int TZ, int L>
-__global__ void __launch_bounds__(TY *TZ, 512 / (TY * TZ))
+__global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
     k_fused_collide_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
                           int nbox, long long total_items, int P, int xl, unsigned int *counter)
 {
