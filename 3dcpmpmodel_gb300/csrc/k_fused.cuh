@@ -372,20 +372,16 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             }
             float lap;
             if (L == 2) {
-                lap = (-r0 * 90.f + (-rm2[c] + rm1[c] * 16.f + rp1[c] * 16.f - rp2[c]) +
-                       (-rc[c - 2 * RZ] + rc[c - RZ] * 16.f + rc[c + RZ] * 16.f - rc[c + 2 * RZ]) +
-                       (-rc[c - 2] + rc[c - 1] * 16.f + rc[c + 1] * 16.f - rc[c + 2])) *
-                      (1.f / 12.f);
+                const float nr = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
+                const float fr = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
+                lap = fmaf(16.f, nr, fmaf(-90.f, r0, -fr)) * (1.f / 12.f);
             } else {
-                lap = (-r0 * 1470.f +
-                       (2.f * rm3[c] - 27.f * rm2[c] + 270.f * rm1[c] + 270.f * rp1[c] - 27.f * rp2[c] + 2.f * rp3[c]) +
-                       (2.f * rc[c - 3 * RZ] - 27.f * rc[c - 2 * RZ] + 270.f * rc[c - RZ] + 270.f * rc[c + RZ] -
-                        27.f * rc[c + 2 * RZ] + 2.f * rc[c + 3 * RZ]) +
-                       (2.f * rc[c - 3] - 27.f * rc[c - 2] + 270.f * rc[c - 1] + 270.f * rc[c + 1] -
-                        27.f * rc[c + 2] + 2.f * rc[c + 3])) *
-                      (1.f / 180.f);
+                const float n1 = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
+                const float n2 = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
+                const float n3 = (rm3[c] + rp3[c]) + (rc[c - 3 * RZ] + rc[c + 3 * RZ]) + (rc[c - 3] + rc[c + 3]);
+                lap = fmaf(270.f, n1, fmaf(-27.f, n2, fmaf(2.f, n3, -1470.f * r0))) * (1.f / 180.f);
             }
-            dst[e] = make_float2(r0, p.kk * mu0_fast(eos, r0) - p.ka * lap);
+            dst[e] = make_float2(r0, fmaf(p.kk, mu0_fast(eos, r0), -p.ka * lap));
         }
     };
 
@@ -488,9 +484,9 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             const float gm[3] = {g0.y * inv360, g1.y * inv360, g2.y * inv360};
             const float gr[3] = {g0.x * inv360, g1.x * inv360, g2.x * inv360};
             const float r = pl[3][mc].x;
-            const float Fx = -gm[0] * r + gr[0] * (1.0f / 3.0f);
-            const float Fy = -gm[1] * r + gr[1] * (1.0f / 3.0f);
-            const float Fz = -gm[2] * r + gr[2] * (1.0f / 3.0f);
+            const float Fx = fmaf(-gm[0], r, gr[0] * (1.0f / 3.0f));
+            const float Fy = fmaf(-gm[1], r, gr[1] * (1.0f / 3.0f));
+            const float Fz = fmaf(-gm[2], r, gr[2] * (1.0f / 3.0f));
 
             // decode with the sources' rest populations as anchors
 
@@ -506,7 +502,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
                 const int sk = gz - cz(q);
                 const bool ss = !yz_fast && p.wall_mode == 1 && (sk < 3 || sk > p.dz - 4);
                 const float a = ss ? a0 : fa[1 - cx(q)][ac - cy(q) * AZ - cz(q)];
-                f[q] = wgt<float>(q) * s2f<S>(hv[q - 1]) + ratio0(q) * a;
+                f[q] = fmaf(wgt<float>(q), s2f<S>(hv[q - 1]), ratio0(q) * a);
             }
             const float ir = 1.0f / r;
             const float ux = (f[1] + f[7] + f[9] + f[11] + f[13] - f[2] - f[8] - f[10] - f[12] - f[14]) * ir;
@@ -534,16 +530,16 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
             f0n[I] = an;
             if (P == 0) {
 #pragma unroll
-                for (int q = 1; q < Q; ++q) *slot(opp(q) - 1, I) = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                for (int q = 1; q < Q; ++q) *slot(opp(q) - 1, I) = f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
             } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
 #pragma unroll
                 for (int q = 1; q < Q; ++q)
                     *slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))) =
-                        f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
             } else {
 #pragma unroll
                 for (int q = 1; q < Q; ++q) {
-                    const S v = f2s<S>((f[q] - ratio0(q) * an) * inv_w(q));
+                    const S v = f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
                     const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy), dk = wrap1(gz + cz(q), p.dz);
                     if (solid_k(p.wall_mode, dk, p.dz))
                         *slot(opp(q) - 1, I) = v;

@@ -283,25 +283,137 @@ __device__ __forceinline__ void collide_mrt_edm(R f[Q], R rho, R ux, R uy, R uz,
     inverse_moments<R>(m, f);
 }
 
-// The same collision for the FUSED kernel with the relaxation written as
-// m* = (1 - s) (m - meq(u)) + meq(u + F/rho): two operations per moment
-// instead of four (mathematically the reference's update; rounding differs).
+// FP32 moment transforms of the FUSED kernel with every fused multiply-add
+// written out (the FUSED translation unit is compiled without implicit
+// contraction, so its rounding does not depend on how the compiler schedules
+// a particular instantiation).  Same algebra as meq_moments / moments /
+// inverse_moments.
+__device__ __forceinline__ void meq_moments_x(float rho, float ux, float uy, float uz, float me[Q])
+{
+    const float uxx = ux * ux, uyy = uy * uy, uzz = uz * uz;
+    const float u2 = uxx + uyy + uzz;
+    const float jx = rho * ux, jy = rho * uy, jz = rho * uz;
+    me[0] = rho;
+    me[1] = rho * fmaf(19.f, u2, -11.f);
+    me[2] = rho * fmaf(-5.5f, u2, 3.f);
+    me[3] = jx;
+    me[4] = jx * (-2.f / 3.f);
+    me[5] = jy;
+    me[6] = jy * (-2.f / 3.f);
+    me[7] = jz;
+    me[8] = jz * (-2.f / 3.f);
+    const float pxx = rho * fmaf(2.f, uxx, -(uyy + uzz));
+    const float pww = rho * (uyy - uzz);
+    me[9] = pxx;
+    me[10] = pxx * -0.5f;
+    me[11] = pww;
+    me[12] = pww * -0.5f;
+    me[13] = jx * uy;
+    me[14] = jy * uz;
+    me[15] = jx * uz;
+    me[16] = me[17] = me[18] = 0.f;
+}
+
+__device__ __forceinline__ void moments_x(const float f[Q], float m[Q])
+{
+    const float a1 = f[1] + f[2], a2 = f[3] + f[4], a3 = f[5] + f[6];
+    const float d1 = f[1] - f[2], d2 = f[3] - f[4], d3 = f[5] - f[6];
+    const float sxy = (f[7] + f[10]) + (f[8] + f[9]);
+    const float xxy = (f[7] - f[10]) - (f[8] - f[9]);
+    const float yxy = (f[7] - f[10]) + (f[8] - f[9]);
+    const float kxy = (f[7] + f[10]) - (f[8] + f[9]);
+    const float sxz = (f[11] + f[14]) + (f[12] + f[13]);
+    const float xxz = (f[11] - f[14]) - (f[12] - f[13]);
+    const float zxz = (f[11] - f[14]) + (f[12] - f[13]);
+    const float kxz = (f[11] + f[14]) - (f[12] + f[13]);
+    const float syz = (f[15] + f[18]) + (f[16] + f[17]);
+    const float yyz = (f[15] - f[18]) - (f[16] - f[17]);
+    const float zyz = (f[15] - f[18]) + (f[16] - f[17]);
+    const float kyz = (f[15] + f[18]) - (f[16] + f[17]);
+    const float es = a1 + a2 + a3, ds = sxy + sxz + syz;
+    m[0] = f[0] + es + ds;
+    m[1] = fmaf(-30.f, f[0], fmaf(-11.f, es, 8.f * ds));
+    m[2] = fmaf(12.f, f[0], fmaf(-4.f, es, ds));
+    const float sx = xxy + xxz, sy = yxy + yyz, sz = zxz + zyz;
+    m[3] = d1 + sx;
+    m[4] = fmaf(-4.f, d1, sx);
+    m[5] = d2 + sy;
+    m[6] = fmaf(-4.f, d2, sy);
+    m[7] = d3 + sz;
+    m[8] = fmaf(-4.f, d3, sz);
+    const float t9 = fmaf(-2.f, syz, sxy + sxz);
+    m[9] = fmaf(2.f, a1, t9 - (a2 + a3));
+    m[10] = fmaf(-4.f, a1, fmaf(2.f, a2 + a3, t9));
+    m[11] = (a2 - a3) + (sxy - sxz);
+    m[12] = fmaf(-2.f, a2 - a3, sxy - sxz);
+    m[13] = kxy;
+    m[14] = kyz;
+    m[15] = kxz;
+    m[16] = xxy - xxz;
+    m[17] = yyz - yxy;
+    m[18] = zxz - zyz;
+}
+
+// f = M^-1 m = M^T (m / norm), the row-norm scalings folded into the
+// fused multiply-adds of the shared partial sums
+__device__ __forceinline__ void inverse_moments_x(const float m[Q], float f[Q])
+{
+    const float n0 = m[0] * (1.f / 19.f), n1 = m[1] * (1.f / 2394.f), n2 = m[2] * (1.f / 252.f);
+    f[0] = fmaf(-30.f, n1, fmaf(12.f, n2, n0));
+    const float be = fmaf(-11.f, n1, fmaf(-4.f, n2, n0));
+    const float bd = fmaf(8.f, n1, n0 + n2);
+    const float jx = fmaf(m[3], 0.1f, m[4] * -0.1f), gx = fmaf(m[3], 0.1f, m[4] * 0.025f);
+    const float jy = fmaf(m[5], 0.1f, m[6] * -0.1f), gy = fmaf(m[5], 0.1f, m[6] * 0.025f);
+    const float jz = fmaf(m[7], 0.1f, m[8] * -0.1f), gz = fmaf(m[7], 0.1f, m[8] * 0.025f);
+    const float pxa = fmaf(m[9], 2.f / 36.f, m[10] * (-4.f / 72.f));
+    const float pyz = fmaf(m[9], -1.f / 36.f, m[10] * (2.f / 72.f));
+    const float qw = fmaf(m[11], 1.f / 12.f, m[12] * (-2.f / 24.f));
+    f[1] = be + jx + pxa;
+    f[2] = be - jx + pxa;
+    f[3] = be + jy + pyz + qw;
+    f[4] = be - jy + pyz + qw;
+    f[5] = be + jz + pyz - qw;
+    f[6] = be - jz + pyz - qw;
+    const float s910 = fmaf(m[9], 1.f / 36.f, m[10] * (1.f / 72.f));
+    const float s1112 = fmaf(m[11], 1.f / 12.f, m[12] * (1.f / 24.f));
+    const float n13 = m[13] * 0.25f, n14 = m[14] * 0.25f, n15 = m[15] * 0.25f;
+    const float n16 = m[16] * 0.125f, n17 = m[17] * 0.125f, n18 = m[18] * 0.125f;
+    const float pxy = bd + s910 + s1112;
+    f[7] = pxy + gx + gy + n13 + n16 - n17;
+    f[8] = pxy - gx + gy - n13 - n16 - n17;
+    f[9] = pxy + gx - gy - n13 + n16 + n17;
+    f[10] = pxy - gx - gy + n13 - n16 + n17;
+    const float pxz = bd + s910 - s1112;
+    f[11] = pxz + gx + gz + n15 - n16 + n18;
+    f[12] = pxz - gx + gz - n15 + n16 + n18;
+    f[13] = pxz + gx - gz - n15 - n16 - n18;
+    f[14] = pxz - gx - gz + n15 + n16 - n18;
+    const float pyzd = fmaf(-2.f, s910, bd);
+    f[15] = pyzd + gy + gz + n14 + n17 - n18;
+    f[16] = pyzd - gy + gz - n14 - n17 - n18;
+    f[17] = pyzd + gy - gz - n14 + n17 + n18;
+    f[18] = pyzd - gy - gz + n14 - n17 + n18;
+}
+
+// The collision of the FUSED kernel: the relaxation written as
+// m* = (1 - s) (m - meq(u)) + meq(u + F/rho), two operations per moment
+// (mathematically the reference's update; rounding differs).
 __device__ __forceinline__ void collide_mrt_edm_fused(float f[Q], float rho, float ux, float uy, float uz,
                                                       float Fx, float Fy, float Fz, const float ts[Q],
                                                       const float omts[Q], const float *qp)
 {
     float m[Q], me[Q], me1[Q];
-    moments<float>(f, m);
-    meq_moments<float>(rho, ux, uy, uz, me);
+    moments_x(f, m);
+    meq_moments_x(rho, ux, uy, uz, me);
     const float ir = 1.0f / rho;
-    meq_moments<float>(rho, ux + Fx * ir, uy + Fy * ir, uz + Fz * ir, me1);
+    meq_moments_x(rho, fmaf(Fx, ir, ux), fmaf(Fy, ir, uy), fmaf(Fz, ir, uz), me1);
 #pragma unroll
     for (int a = 0; a < Q; ++a) {
         float v = a >= 16 ? omts[a] * m[a] : fmaf(omts[a], m[a] - me[a], me1[a]);  // meq = 0 for 16..18
         if (qp) v = fmaf(qp[a], ts[a], v);
         m[a] = v;
     }
-    inverse_moments<float>(m, f);
+    inverse_moments_x(m, f);
 }
 
 }  // namespace cpmp
