@@ -154,13 +154,14 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     const R inv_norm[Q] = {R(1) / R(19), R(1) / R(2394), R(1) / R(252), R(0.1), R(0.025), R(0.1), R(0.025),
                            R(0.1),       R(0.025),       R(1) / R(36),  R(1) / R(72), R(1) / R(12), R(1) / R(24),
                            R(0.25),      R(0.25),        R(0.25),       R(0.125),     R(0.125),     R(0.125)};
-    R am[Q], a0[Q], a1[Q];
+    // y = (1 - S) M lambda*; the adjoint weights of meq(u) and meq(u + F/rho)
+    // are a0 = -diag(1/norm) y and a1 = diag(1/norm) M lambda*
+    R y[Q], a0[Q], a1[Q];
 #pragma unroll
     for (int a = 0; a < Q; ++a) {
-        const R mu_a = ms[a] * inv_norm[a];
-        am[a] = (R(1) - p.ts[a]) * mu_a;
-        a0[a] = (p.ts[a] - R(1)) * mu_a;
-        a1[a] = mu_a;
+        y[a] = p.omts[a] * ms[a];
+        a0[a] = -y[a] * inv_norm[a];
+        a1[a] = ms[a] * inv_norm[a];
     }
     const R r = rho[I], ux = u[I], uy = u[I + n], uz = u[I + 2 * n];
     const R Fx = F[I], Fy = F[I + n], Fz = F[I + 2 * n];
@@ -179,28 +180,23 @@ __global__ void __launch_bounds__(128) k_adj_collide(KParams<R> p, const uint8_t
     const R ajx = aux * ir, ajy = auy * ir, ajz = auz * ir;
     a_rho -= (aux * ux + auy * uy + auz * uz) * ir;
     lamrho[I] = a_rho;
-    // m = M f  ->  M^T am ;  j = sum e f  ->  e . aj
+    // m = M f -> M^T (diag(1/norm) y) = M^-1 y ;  j = sum e f -> e . aj
     R fm[Q];
-    // M^T x = diag(norm) M^-1 x  (M^-1 = M^T diag(1/norm))
-    R amn[Q];
-    const R norm[Q] = {R(19), R(2394), R(252), R(10), R(40), R(10), R(40), R(10), R(40), R(36),
-                       R(72), R(12),   R(24),  R(4),  R(4),  R(4),  R(8),  R(8),  R(8)};
-#pragma unroll
-    for (int a = 0; a < Q; ++a) amn[a] = am[a] * norm[a];
-    inverse_moments<R>(amn, fm);
+    inverse_moments<R>(y, fm);
 #pragma unroll
     for (int q = 0; q < Q; ++q) lamp[q * n + I] = fm[q] + R(cx(q)) * ajx + R(cy(q)) * ajy + R(cz(q)) * ajz;
 }
 
-// R3: force adjoint.  A CTA owns an FT_Y x FT_Z column tile and marches
+// R3: force adjoint.  A CTA owns an FF_Y x FT_Z column tile and marches
 // over FT_X planes of x; the packed (lamF, rho) of planes x-3 .. x+3 with a
 // halo of 3 in y and z sit in an eight-plane shared-memory ring (plane x+4 is
 // copied in with cp.async while plane x is computed), so every one of the 54
 // stencil points of a node is one shared-memory vector load and each global
 // value is loaded once per CTA plus halo.  Periodic wrap in y and z comes from
 // per-CTA coordinate tables, in x from the plane index.
-constexpr int FT_Y = 4, FT_Z = 32, FT_X = 16;
+constexpr int FT_Y = 8, FT_Z = 32, FT_X = 16;  // R4's tile
 constexpr int FH_Y = FT_Y + 6, FH_Z = FT_Z + 6;
+constexpr int FF_Y = 4, FFH_Y = FF_Y + 6;      // R3's tile height (its 16-byte ring rows are larger)
 // CTAs of the tiled R3 / R4 launches
 __host__ __device__ constexpr long long adj_mu_blocks(int dx, int dy, int dz)
 {
@@ -209,23 +205,23 @@ __host__ __device__ constexpr long long adj_mu_blocks(int dx, int dy, int dz)
 template <class R>
 constexpr size_t adj_force_smem()
 {
-    return sizeof(Pack4<R>) * 8 * FH_Y * FH_Z + sizeof(int) * (FH_Y + FH_Z);
+    return sizeof(Pack4<R>) * 8 * FFH_Y * FH_Z + sizeof(int) * (FFH_Y + FH_Z);
 }
 template <class R>
-__global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
+__global__ void __launch_bounds__(FF_Y *FT_Z) k_adj_force(KParams<R> p, const uint8_t *type, const R *gm,
                                                            const Pack4<R> *lamF, R *lammu, Pack2<R> *lmr, R *lamrho)
 {
     extern __shared__ __align__(16) unsigned char fsm[];
     Pack4<R> *ring = reinterpret_cast<Pack4<R> *>(fsm);
-    int *tabY = reinterpret_cast<int *>(ring + 8 * FH_Y * FH_Z);
-    int *tabZ = tabY + FH_Y;
-    constexpr int NT = FT_Y * FT_Z, PL = FH_Y * FH_Z;
-    const int z0 = blockIdx.x * FT_Z, y0 = blockIdx.y * FT_Y, x0 = blockIdx.z * FT_X;
+    int *tabY = reinterpret_cast<int *>(ring + 8 * FFH_Y * FH_Z);
+    int *tabZ = tabY + FFH_Y;
+    constexpr int NT = FF_Y * FT_Z, PL = FFH_Y * FH_Z;
+    const int z0 = blockIdx.x * FT_Z, y0 = blockIdx.y * FF_Y, x0 = blockIdx.z * FT_X;
     const int x1 = min(x0 + FT_X, p.dx);
     const long long n = p.n;
-    for (int e = threadIdx.x; e < FH_Y + FH_Z; e += NT) {
-        if (e < FH_Y) tabY[e] = wrap_off(y0 - 3 + e, p.dy);
-        else tabZ[e - FH_Y] = wrap_off(z0 - 3 + (e - FH_Y), p.dz);
+    for (int e = threadIdx.x; e < FFH_Y + FH_Z; e += NT) {
+        if (e < FFH_Y) tabY[e] = wrap_off(y0 - 3 + e, p.dy);
+        else tabZ[e - FFH_Y] = wrap_off(z0 - 3 + (e - FFH_Y), p.dz);
     }
     __syncthreads();
     auto slot = [](int x) { return x & 7; };
@@ -295,12 +291,12 @@ __global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_force(KParams<R> p, const ui
             acc(P1{}, Z0{}, M1{});
             acc(Z0{}, P1{}, P1{});
             acc(Z0{}, P1{}, M1{});
-            const R lmu = sm / R(360);
+            const R lmu = sm * R(1.0 / 360.0);
             const bool fl = type[I] == FLUID;
             const Pack4<R> own = ring[slot(x) * PL + c];
             lammu[I] = lmu;
             lmr[I] = Pack2<R>{fl ? lmu : R(0), own.w};  // lam_mu on fluid nodes and rho, for R4
-            R add = -sr / R(360) / R(3);
+            R add = -sr * R(1.0 / 1080.0);
             if (fl)  // grad(mu) of the forward step, stored by its replay
                 add -= own.x * gm[I] + own.y * gm[I + n] + own.z * gm[I + 2 * n];
             lamrho[I] += add;
@@ -382,14 +378,14 @@ __global__ void __launch_bounds__(FT_Y *FT_Z) k_adj_mu(KParams<R> p, const uint8
                     lx += w * (a1.x + a2.x + a3.x + a4.x + a5.x + a6.x);
                     ly += w * (a1.y + a2.y + a3.y + a4.y + a5.y + a6.y);
                 }
-                lx /= R(180);
-                ly /= R(180);
+                lx *= R(1.0 / 180.0);
+                ly *= R(1.0 / 180.0);
             } else {
                 auto l5 = [&](auto f) -> R {
                     return (-f(0, 0, 0) * R(90) + (-f(-2, 0, 0) + f(-1, 0, 0) * R(16) + f(1, 0, 0) * R(16) - f(2, 0, 0)) +
                             (-f(0, -2, 0) + f(0, -1, 0) * R(16) + f(0, 1, 0) * R(16) - f(0, 2, 0)) +
-                            (-f(0, 0, -2) + f(0, 0, -1) * R(16) + f(0, 0, 1) * R(16) - f(0, 0, 2))) /
-                           R(12);
+                            (-f(0, 0, -2) + f(0, 0, -1) * R(16) + f(0, 0, 1) * R(16) - f(0, 0, 2))) *
+                           R(1.0 / 12.0);
                 };
                 lx = l5([&](int a, int b, int cc) { return at(a, b, cc).x; });
                 ly = l5([&](int a, int b, int cc) { return at(a, b, cc).y; });
@@ -569,10 +565,12 @@ void adj_launch_step(const KParams<R> &p, const uint8_t *type, const R *rho, con
             cudaFuncSetAttribute(k_adj_mu<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_mu_smem<R>());
             attr_dev = dev;
         }
+        const dim3 gff((unsigned)((p.dz + FT_Z - 1) / FT_Z), (unsigned)((p.dy + FF_Y - 1) / FF_Y),
+                       (unsigned)((p.dx + FT_X - 1) / FT_X));
         const dim3 gf((unsigned)((p.dz + FT_Z - 1) / FT_Z), (unsigned)((p.dy + FT_Y - 1) / FT_Y),
                       (unsigned)((p.dx + FT_X - 1) / FT_X));
         hook_begin(hook, K_ADJ_FORCE, st);
-        k_adj_force<R><<<gf, FT_Y * FT_Z, adj_force_smem<R>(), st>>>(p, type, gm, lamF, b.lammu, b.lmr, b.lamrho);
+        k_adj_force<R><<<gff, FF_Y * FT_Z, adj_force_smem<R>(), st>>>(p, type, gm, lamF, b.lammu, b.lmr, b.lamrho);
         hook_end(hook, K_ADJ_FORCE, st);
         hook_begin(hook, K_ADJ_MU, st);
         k_adj_mu<R><<<gf, FT_Y * FT_Z, adj_mu_smem<R>(), st>>>(p, type, b.lmr, b.lamrho, b.ka_acc);

@@ -416,4 +416,145 @@ __device__ __forceinline__ void collide_mrt_edm_fused(float f[Q], float rho, flo
     inverse_moments_x(m, f);
 }
 
+#ifdef __CUDACC__
+// Two nodes at once (lane x, lane y) with the paired FP32 instructions:
+// the same operations in the same order as the _x versions above, so a pair
+// gives exactly the bits of two single-node evaluations.
+namespace p2 {
+__device__ __forceinline__ float2 K(float c) { return make_float2(c, c); }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+}  // namespace p2
+
+__device__ __forceinline__ void meq_moments_x2(float2 rho, float2 ux, float2 uy, float2 uz, float2 me[Q])
+{
+    using namespace p2;
+    const float2 uxx = mul(ux, ux), uyy = mul(uy, uy), uzz = mul(uz, uz);
+    const float2 u2 = add(add(uxx, uyy), uzz);
+    const float2 jx = mul(rho, ux), jy = mul(rho, uy), jz = mul(rho, uz);
+    me[0] = rho;
+    me[1] = mul(rho, fma(K(19.f), u2, K(-11.f)));
+    me[2] = mul(rho, fma(K(-5.5f), u2, K(3.f)));
+    me[3] = jx;
+    me[4] = mul(jx, K(-2.f / 3.f));
+    me[5] = jy;
+    me[6] = mul(jy, K(-2.f / 3.f));
+    me[7] = jz;
+    me[8] = mul(jz, K(-2.f / 3.f));
+    const float2 pxx = mul(rho, fma(K(2.f), uxx, neg(add(uyy, uzz))));
+    const float2 pww = mul(rho, sub(uyy, uzz));
+    me[9] = pxx;
+    me[10] = mul(pxx, K(-0.5f));
+    me[11] = pww;
+    me[12] = mul(pww, K(-0.5f));
+    me[13] = mul(jx, uy);
+    me[14] = mul(jy, uz);
+    me[15] = mul(jx, uz);
+    me[16] = me[17] = me[18] = K(0.f);
+}
+
+__device__ __forceinline__ void moments_x2(const float2 f[Q], float2 m[Q])
+{
+    using namespace p2;
+    const float2 a1 = add(f[1], f[2]), a2 = add(f[3], f[4]), a3 = add(f[5], f[6]);
+    const float2 d1 = sub(f[1], f[2]), d2 = sub(f[3], f[4]), d3 = sub(f[5], f[6]);
+    const float2 sxy = add(add(f[7], f[10]), add(f[8], f[9]));
+    const float2 xxy = sub(sub(f[7], f[10]), sub(f[8], f[9]));
+    const float2 yxy = add(sub(f[7], f[10]), sub(f[8], f[9]));
+    const float2 kxy = sub(add(f[7], f[10]), add(f[8], f[9]));
+    const float2 sxz = add(add(f[11], f[14]), add(f[12], f[13]));
+    const float2 xxz = sub(sub(f[11], f[14]), sub(f[12], f[13]));
+    const float2 zxz = add(sub(f[11], f[14]), sub(f[12], f[13]));
+    const float2 kxz = sub(add(f[11], f[14]), add(f[12], f[13]));
+    const float2 syz = add(add(f[15], f[18]), add(f[16], f[17]));
+    const float2 yyz = sub(sub(f[15], f[18]), sub(f[16], f[17]));
+    const float2 zyz = add(sub(f[15], f[18]), sub(f[16], f[17]));
+    const float2 kyz = sub(add(f[15], f[18]), add(f[16], f[17]));
+    const float2 es = add(add(a1, a2), a3), ds = add(add(sxy, sxz), syz);
+    m[0] = add(add(f[0], es), ds);
+    m[1] = fma(K(-30.f), f[0], fma(K(-11.f), es, mul(K(8.f), ds)));
+    m[2] = fma(K(12.f), f[0], fma(K(-4.f), es, ds));
+    const float2 sx = add(xxy, xxz), sy = add(yxy, yyz), sz = add(zxz, zyz);
+    m[3] = add(d1, sx);
+    m[4] = fma(K(-4.f), d1, sx);
+    m[5] = add(d2, sy);
+    m[6] = fma(K(-4.f), d2, sy);
+    m[7] = add(d3, sz);
+    m[8] = fma(K(-4.f), d3, sz);
+    const float2 t9 = fma(K(-2.f), syz, add(sxy, sxz));
+    m[9] = fma(K(2.f), a1, sub(t9, add(a2, a3)));
+    m[10] = fma(K(-4.f), a1, fma(K(2.f), add(a2, a3), t9));
+    m[11] = add(sub(a2, a3), sub(sxy, sxz));
+    m[12] = fma(K(-2.f), sub(a2, a3), sub(sxy, sxz));
+    m[13] = kxy;
+    m[14] = kyz;
+    m[15] = kxz;
+    m[16] = sub(xxy, xxz);
+    m[17] = sub(yyz, yxy);
+    m[18] = sub(zxz, zyz);
+}
+
+__device__ __forceinline__ void inverse_moments_x2(const float2 m[Q], float2 f[Q])
+{
+    using namespace p2;
+    const float2 n0 = mul(m[0], K(1.f / 19.f)), n1 = mul(m[1], K(1.f / 2394.f)), n2 = mul(m[2], K(1.f / 252.f));
+    f[0] = fma(K(-30.f), n1, fma(K(12.f), n2, n0));
+    const float2 be = fma(K(-11.f), n1, fma(K(-4.f), n2, n0));
+    const float2 bd = fma(K(8.f), n1, add(n0, n2));
+    const float2 jx = fma(m[3], K(0.1f), mul(m[4], K(-0.1f))), gx = fma(m[3], K(0.1f), mul(m[4], K(0.025f)));
+    const float2 jy = fma(m[5], K(0.1f), mul(m[6], K(-0.1f))), gy = fma(m[5], K(0.1f), mul(m[6], K(0.025f)));
+    const float2 jz = fma(m[7], K(0.1f), mul(m[8], K(-0.1f))), gz = fma(m[7], K(0.1f), mul(m[8], K(0.025f)));
+    const float2 pxa = fma(m[9], K(2.f / 36.f), mul(m[10], K(-4.f / 72.f)));
+    const float2 pyz = fma(m[9], K(-1.f / 36.f), mul(m[10], K(2.f / 72.f)));
+    const float2 qw = fma(m[11], K(1.f / 12.f), mul(m[12], K(-2.f / 24.f)));
+    f[1] = add(add(be, jx), pxa);
+    f[2] = add(sub(be, jx), pxa);
+    f[3] = add(add(add(be, jy), pyz), qw);
+    f[4] = add(add(sub(be, jy), pyz), qw);
+    f[5] = sub(add(add(be, jz), pyz), qw);
+    f[6] = sub(add(sub(be, jz), pyz), qw);
+    const float2 s910 = fma(m[9], K(1.f / 36.f), mul(m[10], K(1.f / 72.f)));
+    const float2 s1112 = fma(m[11], K(1.f / 12.f), mul(m[12], K(1.f / 24.f)));
+    const float2 n13 = mul(m[13], K(0.25f)), n14 = mul(m[14], K(0.25f)), n15 = mul(m[15], K(0.25f));
+    const float2 n16 = mul(m[16], K(0.125f)), n17 = mul(m[17], K(0.125f)), n18 = mul(m[18], K(0.125f));
+    const float2 pxy = add(add(bd, s910), s1112);
+    f[7] = sub(add(add(add(add(pxy, gx), gy), n13), n16), n17);
+    f[8] = sub(sub(sub(add(sub(pxy, gx), gy), n13), n16), n17);
+    f[9] = add(add(sub(sub(add(pxy, gx), gy), n13), n16), n17);
+    f[10] = add(sub(add(sub(sub(pxy, gx), gy), n13), n16), n17);
+    const float2 pxz = sub(add(bd, s910), s1112);
+    f[11] = add(sub(add(add(add(pxz, gx), gz), n15), n16), n18);
+    f[12] = add(add(sub(add(sub(pxz, gx), gz), n15), n16), n18);
+    f[13] = sub(sub(sub(sub(add(pxz, gx), gz), n15), n16), n18);
+    f[14] = sub(add(add(sub(sub(pxz, gx), gz), n15), n16), n18);
+    const float2 pyzd = fma(K(-2.f), s910, bd);
+    f[15] = sub(add(add(add(add(pyzd, gy), gz), n14), n17), n18);
+    f[16] = sub(sub(sub(add(sub(pyzd, gy), gz), n14), n17), n18);
+    f[17] = add(add(sub(sub(add(pyzd, gy), gz), n14), n17), n18);
+    f[18] = add(sub(add(sub(sub(pyzd, gy), gz), n14), n17), n18);
+}
+
+// collide_mrt_edm_fused for two nodes; ir = 1 / rho per lane.
+__device__ __forceinline__ void collide_mrt_edm_fused2(float2 f[Q], float2 rho, float2 ir, float2 ux, float2 uy,
+                                                       float2 uz, float2 Fx, float2 Fy, float2 Fz,
+                                                       const float ts[Q], const float omts[Q], const float2 *qp)
+{
+    using namespace p2;
+    float2 m[Q], me[Q], me1[Q];
+    moments_x2(f, m);
+    meq_moments_x2(rho, ux, uy, uz, me);
+    meq_moments_x2(rho, fma(Fx, ir, ux), fma(Fy, ir, uy), fma(Fz, ir, uz), me1);
+#pragma unroll
+    for (int a = 0; a < Q; ++a) {
+        float2 v = a >= 16 ? mul(K(omts[a]), m[a]) : fma(K(omts[a]), sub(m[a], me[a]), me1[a]);
+        if (qp) v = fma(qp[a], K(ts[a]), v);
+        m[a] = v;
+    }
+    inverse_moments_x2(m, f);
+}
+#endif  // __CUDACC__
+
 }  // namespace cpmp

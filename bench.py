@@ -158,6 +158,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(v: float, ws: int, device: str = "cuda") -> float:
+    """The largest of every rank's value (the whole job waits for the
+    slowest replica); identity for one rank."""
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mlups(nodes_per_rank: int, steps: int, seconds_max: float, ws: int) -> float:
+    """Replicas only: every rank updates its own box of nodes_per_rank nodes,
+    so the job's throughput is ws times one rank's, timed by the slowest."""
+    return nodes_per_rank * steps / seconds_max / 1e6 * ws
+
+
 def run_ours(args) -> None:
     import importlib
 
@@ -205,14 +223,8 @@ def run_ours(args) -> None:
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     launches = s.launch_count - l0
-    ms_max = ms
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    mlups_rank = n * args.steps / (ms_max / 1e3) / 1e6
-    value = mlups_rank * ws
+    ms_max = max_over_ranks(ms, ws)
+    value = whole_job_mlups(n, args.steps, ms_max / 1e3, ws)
 
     # ---- per-kernel timing pass (same workload, events around each launch)
     s.kernel_timing(True)
@@ -269,13 +281,8 @@ def run_ours(args) -> None:
         cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["rho"], cp._abi.CPMP_F32,
                                          host_r.ctypes.data_as(C.c_void_p), C.c_size_t(host_r.nbytes)))
         t1 = time.perf_counter()
-        dt = t1 - t0
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([dt], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-        e2e = {"value": round(n * args.steps / dt / 1e6 * ws, 1), "unit": "MLUPS",
+        dt = max_over_ranks(t1 - t0, ws)
+        e2e = {"value": round(whole_job_mlups(n, args.steps, dt, ws), 1), "unit": "MLUPS",
                "h2d_bytes_per_step": int(host_f.nbytes / args.steps),
                "d2h_bytes_per_step": int((host_r.nbytes + args.steps * C.sizeof(cp.Diag)) / args.steps),
                "what": "cpmp_set_field(DIST, pinned FP32) + K x (cpmp_step(1) + cpmp_reduce) + "
