@@ -1296,16 +1296,23 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     const size_t sstate = 29 * n;   // segment state: f | rho | u | grad mu (3N) | F (3N)
     const int nck = (T + S - 1) / S;
     std::vector<void *> mem;
+    cudaStream_t rs = nullptr;  // replay stream
+    cudaEvent_t replayed[2] = {nullptr, nullptr}, reversed[2] = {nullptr, nullptr}, fwd = nullptr;
     auto alloc = [&](void **p, size_t bytes, const char *what) -> cpmp_status {
         cpmp_status s = dalloc(p, bytes, what);
         if (s == CPMP_OK) mem.push_back(*p);
         return s;
     };
     auto release = [&]() {
+        if (rs) cudaStreamSynchronize(rs);
         for (void *q : mem) cudaFree(q);
         mem.clear();
+        for (cudaEvent_t e : {replayed[0], replayed[1], reversed[0], reversed[1], fwd})
+            if (e) cudaEventDestroy(e);
+        if (rs) cudaStreamDestroy(rs);
+        rs = nullptr;
     };
-    R *ck = nullptr, *seg = nullptr, *mvr = nullptr, *mus = nullptr;
+    R *ck = nullptr, *seg[2] = {nullptr, nullptr}, *mvr = nullptr, *mus = nullptr;
     double *target = nullptr;
     AdjBufs<R> b{};
     const KParams<R> kp = make_kparams<R>(h);
@@ -1318,7 +1325,7 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
         return s;                                                         \
     }
     ALLOC(ck, (size_t)nck * state * sizeof(R), "adjoint checkpoints");
-    ALLOC(seg, (size_t)S * sstate * sizeof(R), "adjoint segment");
+    ALLOC(seg[0], (size_t)S * sstate * sizeof(R), "adjoint segment");
     ALLOC(mvr, 3 * n * sizeof(R), "adjoint mv");
     ALLOC(mus, n * sizeof(R), "adjoint mu");
     ALLOC(target, n * sizeof(double), "adjoint target");
@@ -1335,52 +1342,98 @@ cpmp_status adjoint_run(cpmp_handle *h, int T, int S, const double *target_host,
     ALLOC(b.gwall, 2 * np * sizeof(double), "wall gradient");
     ALLOC(b.loss, sizeof(double), "loss");
 #undef ALLOC
+    // A second segment buffer lets the replay of segment k-1 run on its own
+    // stream while the reverse sweep of segment k runs; without the room for
+    // it the two alternate on one buffer.
+    int nbuf = 1;
+    if (nck > 1 && cudaMalloc((void **)&seg[1], (size_t)S * sstate * sizeof(R)) == cudaSuccess) {
+        mem.push_back(seg[1]);
+        nbuf = 2;
+    }
+    cudaGetLastError();
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking);
+        for (cudaEvent_t *ev : {&replayed[0], &replayed[1], &reversed[0], &reversed[1], &fwd})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            release();
+            return fail(CPMP_ERR_CUDA, std::string("adjoint streams: ") + cudaGetErrorString(e));
+        }
+    }
     cudaStream_t st = h->st;
-    CK(cudaMemcpyAsync(target, target_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(b.gka, 0, sizeof(double), st));
-    CK(cudaMemsetAsync(b.gwall, 0, 2 * np * sizeof(double), st));
+#define CKR(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            release();                                                                             \
+            return fail(CPMP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+        }                                                                                          \
+    } while (0)
+    CKR(cudaMemcpyAsync(target, target_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemsetAsync(b.gka, 0, sizeof(double), st));
+    CKR(cudaMemsetAsync(b.gwall, 0, 2 * np * sizeof(double), st));
     auto save = [&](R *dst) {
         cudaMemcpyAsync(dst, h->fb[h->cur], 19 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(dst + 19 * n, h->rho, n * sizeof(R), cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(dst + 20 * n, h->u, 3 * n * sizeof(R), cudaMemcpyDeviceToDevice, st);
     };
     LaunchHook *hook = h->timing ? h->hook.get() : nullptr;
-    // forward, checkpoint every S steps (the handle's own state advances to T)
-    for (int t = 0; t < T; ++t) {
-        if (t % S == 0) save(ck + (size_t)(t / S) * state);
-        launch_one_step(h, hook);
-    }
-    adj_launch_loss<R>(kp, h->type, (const R *)h->rho, target, b, st);
-    CK(cudaGetLastError());
-    // reverse sweep, one segment at a time
-    for (int kseg = nck - 1; kseg >= 0; --kseg) {
-        const int n0 = kseg * S, n1 = std::min(n0 + S, T), len = n1 - n0;
-        cudaMemcpyAsync(seg, ck + (size_t)kseg * state, state * sizeof(R), cudaMemcpyDeviceToDevice, st);
-        // replay the forward inside the segment: the step from state m-1 to m
-        // extrapolates the wall layers of state m-1's density in place and
-        // leaves its grad mu and F in its slot, so each slot ends up holding
-        // what the reverse step needs (walled rho, u, grad mu, F)
+    // Replay segment k on the replay stream into buffer k % nbuf: the step
+    // from state m-1 to m extrapolates the wall layers of state m-1's density
+    // in place and leaves its grad mu and F in its slot, so each slot ends up
+    // holding what the reverse step needs (walled rho, u, grad mu, F).
+    auto replay = [&](int k) {
+        const int n0 = k * S, len = std::min(n0 + S, T) - n0, bi = k % nbuf;
+        if (k + nbuf < nck) cudaStreamWaitEvent(rs, reversed[bi], 0);  // the buffer's previous segment is done
+        R *sg = seg[bi];
+        cudaMemcpyAsync(sg, ck + (size_t)k * state, state * sizeof(R), cudaMemcpyDeviceToDevice, rs);
         for (int m = 1; m < len; ++m) {
-            R *prev = seg + (size_t)(m - 1) * sstate, *cur = seg + (size_t)m * sstate;
+            R *prev = sg + (size_t)(m - 1) * sstate, *cur = sg + (size_t)m * sstate;
             plain_launch_step_split<R, R>(kp, h->type, prev + 19 * n, mus, prev + 20 * n, prev + 26 * n, mvr, prev,
-                                          cur, cur + 19 * n, cur + 20 * n, prev + 23 * n, st, hook);
+                                          cur, cur + 19 * n, cur + 20 * n, prev + 23 * n, rs, hook);
         }
-        {   // the last state of the segment is never stepped from
-            R *last = seg + (size_t)(len - 1) * sstate;
-            plain_launch_mu_force<R>(kp, h->type, last + 19 * n, mus, last + 26 * n, st, last + 23 * n);
-        }
+        R *last = sg + (size_t)(len - 1) * sstate;  // never stepped from
+        plain_launch_mu_force<R>(kp, h->type, last + 19 * n, mus, last + 26 * n, rs, last + 23 * n);
+        cudaEventRecord(replayed[bi], rs);
+    };
+    auto reverse = [&](int k) {
+        const int n0 = k * S, n1 = std::min(n0 + S, T), bi = k % nbuf;
+        cudaStreamWaitEvent(st, replayed[bi], 0);
         for (int t = n1 - 1; t >= n0; --t) {
-            const R *stt = seg + (size_t)(t - n0) * sstate;
+            const R *stt = seg[bi] + (size_t)(t - n0) * sstate;
             adj_launch_step<R>(kp, h->type, stt + 19 * n, stt + 20 * n, stt + 23 * n, stt + 26 * n, b, st, hook);
             std::swap(b.lamp, b.lamp_next);
             std::swap(b.lamrho, b.lamrho_next);
         }
+        cudaEventRecord(reversed[bi], st);
+    };
+    // forward, checkpoint every S steps (the handle's own state advances to
+    // T); the last segment's replay starts as soon as its checkpoint exists
+    for (int t = 0; t < T; ++t) {
+        if (t % S == 0) {
+            save(ck + (size_t)(t / S) * state);
+            if (t / S == nck - 1) {
+                cudaEventRecord(fwd, st);
+                cudaStreamWaitEvent(rs, fwd, 0);
+                replay(nck - 1);
+            }
+        }
+        launch_one_step(h, hook);
+    }
+    adj_launch_loss<R>(kp, h->type, (const R *)h->rho, target, b, st);
+    CKR(cudaGetLastError());
+    // reverse sweep, one segment at a time, the next segment's replay ahead
+    for (int k = nck - 1; k >= 0; --k) {
+        if (nbuf == 2 && k > 0) replay(k - 1);
+        reverse(k);
+        if (nbuf == 1 && k > 0) replay(k - 1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             release();
             return fail(CPMP_ERR_CUDA, std::string("adjoint sweep: ") + cudaGetErrorString(e));
         }
     }
+#undef CKR
     adj_launch_finish<R>(kp, b, st);
     std::vector<double> gw(2 * np);
     double loss = 0, gka = 0;
