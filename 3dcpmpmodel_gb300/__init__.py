@@ -226,10 +226,20 @@ class Solver:
         on a scratch copy of the current state."""
         ty, tz, xl, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         _abi.check(self._lib.cpmp_autotune(self._h, C.byref(ty), C.byref(tz), C.byref(xl), C.byref(ms)))
-        return {"tile_y": ty.value, "tile_z": tz.value, "march_x": xl.value, "collide_ms": ms.value}
+        t = self.tile()
+        t["collide_ms"] = ms.value
+        return t
 
-    def set_tile(self, tile_y: int, tile_z: int, march_x: int):
-        _abi.check(self._lib.cpmp_set_tile(self._h, int(tile_y), int(tile_z), int(march_x)))
+    def set_tile(self, tile_y: int, tile_z: int, march_x: int, nodes_per_thread: int = 1):
+        """Column tile (tile_y x tile_z nodes), x-march length and nodes per
+        thread (1, or 2 for the paired kernel) of the fused collide."""
+        _abi.check(self._lib.cpmp_set_tile_ex(self._h, int(tile_y), int(tile_z), int(march_x),
+                                              int(nodes_per_thread)))
+
+    def tile(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        _abi.check(self._lib.cpmp_get_tile(self._h, *(C.byref(x) for x in v)))
+        return dict(zip(("tile_y", "tile_z", "march_x", "nodes_per_thread"), (x.value for x in v)))
 
     # timing ------------------------------------------------------------------------
     @property
@@ -277,14 +287,22 @@ class Batch:
     def sync(self):
         _abi.check(self._lib.cpmp_batch_sync(self._b))
 
-    def set_tile(self, tile_y: int, tile_z: int, march_x: int):
-        _abi.check(self._lib.cpmp_batch_set_tile(self._b, int(tile_y), int(tile_z), int(march_x)))
+    def set_tile(self, tile_y: int, tile_z: int, march_x: int, nodes_per_thread: int = 1):
+        _abi.check(self._lib.cpmp_batch_set_tile_ex(self._b, int(tile_y), int(tile_z), int(march_x),
+                                                    int(nodes_per_thread)))
+
+    def tile(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        _abi.check(self._lib.cpmp_batch_get_tile(self._b, *(C.byref(x) for x in v)))
+        return dict(zip(("tile_y", "tile_z", "march_x", "nodes_per_thread"), (x.value for x in v)))
 
     def autotune(self) -> dict:
         ty, tz, xl, ms = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         _abi.check(self._lib.cpmp_batch_autotune(self._b, C.byref(ty), C.byref(tz), C.byref(xl),
                                                  C.byref(ms)))
-        return {"tile_y": ty.value, "tile_z": tz.value, "march_x": xl.value, "step_ms": ms.value}
+        t = self.tile()
+        t["step_ms"] = ms.value
+        return t
 
     @property
     def stream(self) -> int:

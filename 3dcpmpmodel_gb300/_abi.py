@@ -85,6 +85,8 @@ SIGNATURES = {
     "cpmp_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "cpmp_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "cpmp_set_tile_ex": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "cpmp_get_tile": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 4),
     "cpmp_stream": (C.c_void_p, [C.c_void_p]),
     "cpmp_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
@@ -104,6 +106,8 @@ SIGNATURES = {
     "cpmp_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
     "cpmp_batch_sync": (C.c_int, [C.c_void_p]),
     "cpmp_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "cpmp_batch_set_tile_ex": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "cpmp_batch_get_tile": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 4),
     "cpmp_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "cpmp_batch_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),

@@ -810,7 +810,7 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     for (int t = 0; t < fused_tile_count(); ++t) {
         for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
-            if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz)) continue;
+            if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz, ft.np)) continue;
             if (ft.xl > h->p.dx && xi > 0) continue;
             if (ft.ty > 2 * h->p.dy && ft.ty > 1) continue;
             if (ft.tz > 2 * h->p.dz) continue;
@@ -846,7 +846,7 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     cudaFree(sf0b);
     cudaFree(srho);
     CK(cudaGetLastError());
-    if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl) {
+    if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl || best.np != h->tile.np) {
         h->tile = best;
         if (h->gexec) {
             cudaGraphExecDestroy(h->gexec);
@@ -862,12 +862,29 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
 
 cpmp_status cpmp_set_tile(cpmp_handle *h, int tile_y, int tile_z, int march_x)
 {
+    return cpmp_set_tile_ex(h, tile_y, tile_z, march_x, 1);
+}
+
+cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    if (h->plain) return fail(CPMP_ERR_UNSUPPORTED, "tiles apply to the FUSED scheme");
+    if (tile_y) *tile_y = h->tile.ty;
+    if (tile_z) *tile_z = h->tile.tz;
+    if (march_x) *march_x = h->tile.xl;
+    if (nodes_per_thread) *nodes_per_thread = h->tile.np;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread)
+{
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
     if (h->plain) return fail(CPMP_ERR_UNSUPPORTED, "tiles apply to the FUSED scheme");
     if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
-    if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z))
+    if (nodes_per_thread != 1 && nodes_per_thread != 2) return fail(CPMP_ERR_PARAM, "nodes_per_thread must be 1 or 2");
+    if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z, nodes_per_thread))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
-    h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx)};
+    h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx), nodes_per_thread};
     if (h->gexec) {
         cudaGraphExecDestroy(h->gexec);
         h->gexec = nullptr;
@@ -943,7 +960,7 @@ cpmp_status batch_upload(cpmp_batch *b)
         b->nodes += h->n;
         b->max_dx = std::max(b->max_dx, h->p.dx);
         b->max_cols = std::max(b->max_cols, (long long)h->p.dx * h->p.dy);
-        b->max_pairs = std::max(b->max_pairs, (long long)h->p.dy * (h->p.dz / 2 + 1));
+        b->max_pairs = std::max(b->max_pairs, (long long)h->p.dy * ((h->p.dz + 1) / 2));
     }
     b->total_items = item;
     CK(cudaMemcpyAsync(b->d_params, kp.data(), nb * sizeof(KParams<float>), cudaMemcpyHostToDevice, b->st));
@@ -1116,11 +1133,27 @@ cpmp_status cpmp_batch_sync(cpmp_batch *b)
 
 cpmp_status cpmp_batch_set_tile(cpmp_batch *b, int tile_y, int tile_z, int march_x)
 {
+    return cpmp_batch_set_tile_ex(b, tile_y, tile_z, march_x, 1);
+}
+
+cpmp_status cpmp_batch_get_tile(cpmp_batch *b, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread)
+{
+    if (!b) return fail(CPMP_ERR_PARAM, "null batch");
+    if (tile_y) *tile_y = b->tile.ty;
+    if (tile_z) *tile_z = b->tile.tz;
+    if (march_x) *march_x = b->tile.xl;
+    if (nodes_per_thread) *nodes_per_thread = b->tile.np;
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_set_tile_ex(cpmp_batch *b, int tile_y, int tile_z, int march_x, int nodes_per_thread)
+{
     if (!b) return fail(CPMP_ERR_PARAM, "null batch");
     if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
-    if (!fused_tile_usable(b->storage, b->lap_order, tile_y, tile_z))
+    if (nodes_per_thread != 1 && nodes_per_thread != 2) return fail(CPMP_ERR_PARAM, "nodes_per_thread must be 1 or 2");
+    if (!fused_tile_usable(b->storage, b->lap_order, tile_y, tile_z, nodes_per_thread))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
-    b->tile = FusedTile{tile_y, tile_z, march_x};
+    b->tile = FusedTile{tile_y, tile_z, march_x, nodes_per_thread};
     for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
     for (cpmp_handle *h : b->boxes) h->tile = b->tile;
     if (b->gexec) {
@@ -1182,7 +1215,7 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
     for (int t = 0; t < fused_tile_count() && err == cudaSuccess; ++t) {
         for (int xi = 0; xi < 4; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
-            if (!fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz)) continue;
+            if (!fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz, ft.np)) continue;
             b->tile = ft;
             for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
             if (batch_upload(b) != CPMP_OK) break;

@@ -110,7 +110,9 @@ __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, con
 
 // ------------------------------------------------------------- dispatch ----
 namespace {
-constexpr int kTiles[][2] = {{4, 32}, {8, 32}, {16, 32}, {2, 64}, {1, 128}};
+// (ty, tz, nodes per thread)
+constexpr int kTiles[][3] = {{4, 32, 1}, {8, 32, 1}, {16, 32, 1}, {2, 64, 1}, {1, 128, 1},
+                             {8, 32, 2}, {16, 32, 2}, {8, 64, 2}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
 template <class F>
@@ -144,14 +146,21 @@ void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, 
     else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, st);
 }
 
+bool fused2_set_attr(int storage, int lap_order, int ty, int tz, int max_smem)
+{
+    if (storage == CPMP_STORE_F16) return fused2_set_attr_f16(lap_order, ty, tz, max_smem);
+    if (storage == CPMP_STORE_BF16) return fused2_set_attr_bf16(lap_order, ty, tz, max_smem);
+    return fused2_set_attr_f32(lap_order, ty, tz, max_smem);
+}
+
 // usable[storage index][L - 2][tile index]: the instantiation's shared
 // memory fits the device's opt-in limit
-bool g_usable[3][2][8];
+bool g_usable[3][2][kNumTiles];
 int storage_index(int storage) { return storage == CPMP_STORE_F16 ? 0 : (storage == CPMP_STORE_BF16 ? 1 : 2); }
-int tile_index(int ty, int tz)
+int tile_index(int ty, int tz, int np = 1)
 {
     for (int i = 0; i < kNumTiles; ++i)
-        if (kTiles[i][0] == ty && kTiles[i][1] == tz) return i;
+        if (kTiles[i][0] == ty && kTiles[i][1] == tz && kTiles[i][2] == np) return i;
     return -1;
 }
 
@@ -179,20 +188,15 @@ void set_attr_l(int si, int max_smem)
 }
 }  // namespace
 
-bool fused_tile_usable(int storage, int lap_order, int ty, int tz)
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np)
 {
-    const int t = tile_index(ty, tz);
+    const int t = tile_index(ty, tz, np);
     return t >= 0 && g_usable[storage_index(storage)][lap_order == 7 ? 1 : 0][t];
 }
 
 int fused_tile_count() { return kNumTiles; }
-FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl}; }
-bool fused_tile_supported(int ty, int tz)
-{
-    for (int i = 0; i < kNumTiles; ++i)
-        if (kTiles[i][0] == ty && kTiles[i][1] == tz) return true;
-    return false;
-}
+FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl, kTiles[idx][2]}; }
+bool fused_tile_supported(int ty, int tz, int np) { return tile_index(ty, tz, np) >= 0; }
 
 cudaError_t fused_setup_attributes()
 {
@@ -206,6 +210,13 @@ cudaError_t fused_setup_attributes()
     set_attr_l<__nv_bfloat16, 3>(1, max_smem);
     set_attr_l<float, 2>(2, max_smem);
     set_attr_l<float, 3>(2, max_smem);
+    const int storages[3] = {CPMP_STORE_F16, CPMP_STORE_BF16, CPMP_STORE_F32};
+    for (int i = 0; i < kNumTiles; ++i) {
+        if (kTiles[i][2] != 2) continue;
+        for (int si = 0; si < 3; ++si)
+            for (int l = 0; l < 2; ++l)
+                g_usable[si][l][i] = fused2_set_attr(storages[si], l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem);
+    }
     return cudaSuccess;
 }
 
@@ -237,24 +248,32 @@ void fused_launch_collide(int storage, const KParams<float> &p, int P, const Fus
                           LaunchHook *hook)
 {
     hook_begin(hook, K_FUSED, st);
-    with_storage(storage, [&](auto tag) {
-        using S = decltype(tag);
-        if (p.lap_order == 7)
-            launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, st);
-        else
-            launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, st);
-    });
+    if (t.np == 2 && storage == CPMP_STORE_F16)
+        fused2_launch_f16(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.np == 2 && storage == CPMP_STORE_BF16)
+        fused2_launch_bf16(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.np == 2)
+        fused2_launch_f32(p, P, t, h, f0c, f0n, rho, st);
+    else
+        with_storage(storage, [&](auto tag) {
+            using S = decltype(tag);
+            if (p.lap_order == 7)
+                launch_collide_l<S, 3>(p, P, t, (S *)h, f0c, f0n, rho, st);
+            else
+                launch_collide_l<S, 2>(p, P, t, (S *)h, f0c, f0n, rho, st);
+        });
     hook_end(hook, K_FUSED, st);
 }
 
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
                           const float *f0, float *rho, cudaStream_t st, LaunchHook *hook)
 {
-    const dim3 g((unsigned)((p.dz / 2 + 1 + 127) / 128), (unsigned)p.dy, (unsigned)p.dx);
+    const dim3 g((unsigned)((pairs_per_column(p.dz) + DENSITY_BZ - 1) / DENSITY_BZ),
+                 (unsigned)((p.dy + DENSITY_BY - 1) / DENSITY_BY), (unsigned)p.dx);
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density<S><<<g, 128, 0, st>>>(p, P, (const S *)h, f0, rho);
+        k_density<S><<<g, dim3(DENSITY_BZ, DENSITY_BY), 0, st>>>(p, P, (const S *)h, f0, rho);
     });
     hook_end(hook, K_DENSITY, st);
 }
@@ -303,13 +322,20 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     }
     hook_begin(hook, K_FUSED, st);
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    with_storage(storage, [&](auto tag) {
-        using S = decltype(tag);
-        if (lap_order == 7)
-            batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
-        else
-            batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
-    });
+    if (t.np == 2 && storage == CPMP_STORE_F16)
+        fused2_batch_f16(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
+    else if (t.np == 2 && storage == CPMP_STORE_BF16)
+        fused2_batch_bf16(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
+    else if (t.np == 2)
+        fused2_batch_f32(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
+    else
+        with_storage(storage, [&](auto tag) {
+            using S = decltype(tag);
+            if (lap_order == 7)
+                batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
+            else
+                batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
+        });
     hook_end(hook, K_FUSED, st);
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {

@@ -229,22 +229,28 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
 
 // First node of the pair thread t of column (i, j) handles: pairs start on
 // even node indices, so a column whose first index is odd begins with a lone
-// node (k0 = -1).
+// node (k0 = -1).  An even DZ makes every column start on an even index
+// (DZ / 2 pairs); an odd one needs (DZ + 1) / 2 pairs whichever the parity.
 __device__ __forceinline__ int pair_k0(const KParams<float> &p, int i, int j, int t)
 {
     const long long base = ((long long)i * p.dy + j) * p.dz;
     return 2 * t - (int)(base & 1);
 }
-__device__ __forceinline__ int pairs_per_column(int dz) { return dz / 2 + 1; }
+__host__ __device__ __forceinline__ int pairs_per_column(int dz) { return (dz + 1) / 2; }
 
-// Grid: (pair blocks, dy, dx); thread t of a column handles one pair.
+// Block: 32 pairs of a column x 4 columns (y); grid (pair blocks, y blocks,
+// dx).  The anchors of the y +- 1 neighbours of a block's nodes are mostly
+// rows that the same block reads, so they come from L1.
+constexpr int DENSITY_BZ = 32, DENSITY_BY = 4;
 template <class S>
-__global__ void __launch_bounds__(128) k_density(KParams<float> p, int P, const S *__restrict__ h,
-                                                 const float *__restrict__ f0, float *__restrict__ rho)
+__global__ void __launch_bounds__(DENSITY_BZ *DENSITY_BY) k_density(KParams<float> p, int P,
+                                                                     const S *__restrict__ h,
+                                                                     const float *__restrict__ f0,
+                                                                     float *__restrict__ rho)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= pairs_per_column(p.dz)) return;
-    const int i = blockIdx.z, j = blockIdx.y;
+    const int t = blockIdx.x * DENSITY_BZ + threadIdx.x, j = blockIdx.y * DENSITY_BY + threadIdx.y;
+    if (t >= pairs_per_column(p.dz) || j >= p.dy) return;
+    const int i = blockIdx.z;
     density_pair<S>(p, P, h, f0, rho, i, j, pair_k0(p, i, j, t));
 }
 
@@ -400,6 +406,15 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
 #pragma unroll
             for (int q = 1; q < Q; ++q)
                 hv[q - 1] = *slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
+        } else if (p.wall_mode == 1 && gy >= 1 && gy + 1 < p.dy && gx >= 1 && gx + 1 < p.dx) {
+            // no wrap: only the sources across a wall layer (z = 3 or dz - 4) are solid
+            const bool lo = gz == 3, hi = gz == p.dz - 4;
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const bool ss = (cz(q) == 1 && lo) || (cz(q) == -1 && hi);
+                hv[q - 1] = *(ss ? slot(q - 1, I)
+                                 : slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))));
+            }
         } else {
 #pragma unroll
             for (int q = 1; q < Q; ++q) {
@@ -536,6 +551,14 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
                 for (int q = 1; q < Q; ++q)
                     *slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))) =
                         f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+            } else if (p.wall_mode == 1 && gy >= 1 && gy + 1 < p.dy && gx >= 1 && gx + 1 < p.dx) {
+                const bool lo = gz == 3, hi = gz == p.dz - 4;
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const bool ss = (cz(q) == -1 && lo) || (cz(q) == 1 && hi);
+                    *(ss ? slot(opp(q) - 1, I) : slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)))) =
+                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                }
             } else {
 #pragma unroll
                 for (int q = 1; q < Q; ++q) {

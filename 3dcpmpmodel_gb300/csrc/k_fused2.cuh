@@ -1,0 +1,485 @@
+// k_fused2.cuh -- the FUSED collide with two z-adjacent nodes per thread.
+//
+// Same storage, A-A addressing, shared-memory rings and arithmetic as
+// fused_tile (k_fused.cuh); a thread owns the node pair (z, z + 1) of its
+// (y, z) column tile, z even.  The collision, decode, encode and velocity
+// run as paired FP32 instructions (FFMA2 / FADD2 / FMUL2) through the _x2
+// moment transforms, which perform the single-node operations in the same
+// order, so a pair gives exactly the bits of two single-node evaluations.
+// With an even DZ every node pair starts on an even node index: the
+// populations of the pair are one 32-bit (FP16 / BF16) or 64-bit (FP32)
+// access wherever the source or destination offset keeps that parity, two
+// scalar accesses where it does not (odd z offsets of the A-A odd step, and
+// every access of a box with an odd DZ).  Pairs next to a wall or a periodic
+// edge take a per-node general path for their global-memory accesses.
+#pragma once
+
+#include "k_fused.cuh"
+
+namespace cpmp {
+
+template <class S>
+struct SPair;
+template <>
+struct SPair<__half> {
+    using T = __half2;
+    static __device__ __forceinline__ float2 tof(T v) { return __half22float2(v); }
+    static __device__ __forceinline__ T fromf(float2 v) { return __float22half2_rn(v); }
+    static __device__ __forceinline__ T make(__half a, __half b) { return __halves2half2(a, b); }
+    static __device__ __forceinline__ __half lo(T v) { return __low2half(v); }
+    static __device__ __forceinline__ __half hi(T v) { return __high2half(v); }
+    static __device__ __forceinline__ __half zero() { return __float2half_rn(0.f); }
+};
+template <>
+struct SPair<__nv_bfloat16> {
+    using T = __nv_bfloat162;
+    static __device__ __forceinline__ float2 tof(T v) { return __bfloat1622float2(v); }
+    static __device__ __forceinline__ T fromf(float2 v) { return __float22bfloat162_rn(v); }
+    static __device__ __forceinline__ T make(__nv_bfloat16 a, __nv_bfloat16 b) { return __halves2bfloat162(a, b); }
+    static __device__ __forceinline__ __nv_bfloat16 lo(T v) { return __low2bfloat16(v); }
+    static __device__ __forceinline__ __nv_bfloat16 hi(T v) { return __high2bfloat16(v); }
+    static __device__ __forceinline__ __nv_bfloat16 zero() { return __float2bfloat16_rn(0.f); }
+};
+template <>
+struct SPair<float> {
+    using T = float2;
+    static __device__ __forceinline__ float2 tof(T v) { return v; }
+    static __device__ __forceinline__ T fromf(float2 v) { return v; }
+    static __device__ __forceinline__ T make(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ float lo(T v) { return v.x; }
+    static __device__ __forceinline__ float hi(T v) { return v.y; }
+    static __device__ __forceinline__ float zero() { return 0.f; }
+};
+
+// Shared-memory geometry of a TY x TZ node tile (TZ even, TY * TZ / 2
+// threads).  As FusedGeom, except that the rest-population ring has a z halo
+// of 2 so that every node pair sits on an even (8-byte aligned) index.
+template <int TY, int TZ, int L>
+struct FusedGeom2 {
+    static_assert(TZ % 2 == 0, "node pairs need an even tile height");
+    static constexpr int RH = 3 + L;
+    static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
+    static constexpr int NR = 8;
+    static_assert(2 * L + 2 <= NR, "rho ring too small");
+    static constexpr int MY = TY + 6, MZ = TZ + 6;
+    static constexpr int AY = TY + 2, AZ = TZ + 4;
+    static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
+    static constexpr int RM_PAIRS = 8 * MY * MZ;
+    static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
+    static constexpr int TAB_INTS = 2 * RY + RZ;
+    static constexpr size_t BYTES = ((sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
+                                      sizeof(float) * F0_FLOATS + sizeof(int) * TAB_INTS + 15) / 16) * 16;
+    static constexpr int THREADS = TY * TZ / 2;
+};
+
+// One CTA owns a TY x TZ column tile and marches over xl planes of x; see
+// fused_tile for the rings and the order of work per plane.
+template <class S, int TY, int TZ, int L>
+__device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, S *__restrict__ h,
+                                            const float *__restrict__ f0c, float *__restrict__ f0n,
+                                            const float *__restrict__ rho, const int z0, const int y0,
+                                            const int x0, const int xl, float4 *smem4)
+{
+    using G = FusedGeom2<TY, TZ, L>;
+    using SP = SPair<S>;
+    using T = typename SP::T;
+    using namespace p2;
+    constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
+    constexpr int AY = G::AY, AZ = G::AZ;
+    constexpr int NT = G::THREADS, TH = TZ / 2;
+    float *srho = reinterpret_cast<float *>(smem4);
+    float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
+    float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
+    int *tabY = reinterpret_cast<int *>(sf0 + G::F0_FLOATS);
+    int *tabZ = tabY + RY;
+    int *tabYdz = tabZ + RZ;
+
+    const int tz = 2 * (threadIdx.x % TH), ty = threadIdx.x / TH;
+    const int x1 = min(x0 + xl, p.dx);
+    const unsigned plane = (unsigned)(p.dy * p.dz);
+    const unsigned n = (unsigned)p.n;
+    auto slot = [&](int q, unsigned idx) -> S * { return h + (size_t)n * (unsigned)q + idx; };
+    const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
+    const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
+
+    for (int e = threadIdx.x; e < RY + RZ; e += NT) {
+        if (e < RY) {
+            tabY[e] = wrap_small(y0 - RH + e, p.dy);
+            tabYdz[e] = tabY[e] * p.dz;
+        } else {
+            tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+        }
+    }
+    __syncthreads();
+
+    auto issue_rho = [&](int xlog) {
+        const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
+        float *dst = srho + (xlog & (NR - 1)) * (RY * RZ);
+        for (int e = threadIdx.x; e < RY * RZ; e += NT) {
+            const int ly = e / RZ, lz = e - ly * RZ;
+            cp_async4(dst + e, src + (unsigned)(tabYdz[ly] + tabZ[lz]));
+        }
+    };
+    // anchors: y halo 1, z halo 2 (column lz is z0 - 2 + lz)
+    auto issue_f0 = [&](int xlog) {
+        const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
+        float *dst = sf0 + (xlog & 3) * (AY * AZ);
+        for (int e = threadIdx.x; e < AY * AZ; e += NT) {
+            const int ly = e / AZ, lz = e - ly * AZ;
+            cp_async4(dst + e, src + (unsigned)(tabYdz[ly + RH - 1] + tabZ[lz + RH - 2]));
+        }
+    };
+    auto comp_mu = [&](int xlog) {
+        const int gx = wrap_small(xlog, p.dx);
+        float2 *dst = srm + (xlog & 7) * (MY * MZ);
+        auto rpl = [&](int xx) -> const float * { return srho + (xx & (NR - 1)) * (RY * RZ); };
+        const float *rc = rpl(xlog), *rm1 = rpl(xlog - 1), *rp1 = rpl(xlog + 1);
+        const float *rm2 = rpl(xlog - 2), *rp2 = rpl(xlog + 2);
+        const float *rm3 = L == 3 ? rpl(xlog - 3) : rc;
+        const float *rp3 = L == 3 ? rpl(xlog + 3) : rc;
+        for (int e = threadIdx.x; e < MY * MZ; e += NT) {
+            const int my = e / MZ, mz = e - my * MZ;
+            const int c = (my + L) * RZ + (mz + L);
+            const float r0 = rc[c];
+            const int gz = tabZ[mz + L];
+            if (solid_k(p.wall_mode, gz, p.dz)) {
+                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : p.dx * p.dy) + gx * p.dy + tabY[my + L]]);
+                continue;
+            }
+            float lap;
+            if (L == 2) {
+                const float nr = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
+                const float fr = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
+                lap = fmaf(16.f, nr, fmaf(-90.f, r0, -fr)) * (1.f / 12.f);
+            } else {
+                const float n1 = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
+                const float n2 = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
+                const float n3 = (rm3[c] + rp3[c]) + (rc[c - 3 * RZ] + rc[c + 3 * RZ]) + (rc[c - 3] + rc[c + 3]);
+                lap = fmaf(270.f, n1, fmaf(-27.f, n2, fmaf(2.f, n3, -1470.f * r0))) * (1.f / 180.f);
+            }
+            dst[e] = make_float2(r0, fmaf(p.kk, mu0_fast(eos, r0), -p.ka * lap));
+        }
+    };
+
+    const int gy = y0 + ty, gz = z0 + tz;
+    const bool inA = gy < p.dy && gz < p.dz && !solid_k(p.wall_mode, gz, p.dz);
+    const bool inB = gy < p.dy && gz + 1 < p.dz && !solid_k(p.wall_mode, gz + 1, p.dz);
+    const bool any = inA || inB, both = inA && inB;
+    const bool ev = (p.dz & 1) == 0;  // every pair starts on an even node index
+
+    // one population of node (gx, gy, gzl) through the general A-A read
+    auto load_general = [&](int q, int gx, int gzl, unsigned Il) -> S {
+        const int si = wrap1(gx - cx(q), p.dx), sj = wrap1(gy - cy(q), p.dy), sk = wrap1(gzl - cz(q), p.dz);
+        if (solid_k(p.wall_mode, sk, p.dz)) return *slot(q - 1, Il);
+        return *slot(opp(q) - 1, (unsigned)si * plane + (unsigned)(sj * p.dz + sk));
+    };
+    auto store_general = [&](int q, int gx, int gzl, unsigned Il, S v) {
+        const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy), dk = wrap1(gzl + cz(q), p.dz);
+        if (solid_k(p.wall_mode, dk, p.dz))
+            *slot(opp(q) - 1, Il) = v;
+        else
+            *slot(q - 1, (unsigned)di * plane + (unsigned)(dj * p.dz + dk)) = v;
+    };
+
+    // moving populations of the pair in plane x into registers
+    auto fetch = [&](int x, T hv[Q - 1]) {
+        if (!any) return;
+        const int gx = wrap_small(x, p.dx);
+        const unsigned I = (unsigned)gx * plane + (unsigned)(gy * p.dz + gz);
+        if (P == 0) {
+            if (ev && both) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) hv[q - 1] = *reinterpret_cast<const T *>(slot(q - 1, I));
+            } else {
+#pragma unroll
+                for (int q = 1; q < Q; ++q)
+                    hv[q - 1] = SP::make(inA ? *slot(q - 1, I) : SP::zero(), inB ? *slot(q - 1, I + 1) : SP::zero());
+            }
+        } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
+            if (ev) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const S *ptr = slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
+                    hv[q - 1] = (cz(q) & 1) ? SP::make(ptr[0], ptr[1]) : *reinterpret_cast<const T *>(ptr);
+                }
+            } else {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const S *ptr = slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
+                    hv[q - 1] = SP::make(ptr[0], ptr[1]);
+                }
+            }
+        } else if (p.wall_mode == 1 && gy >= 1 && gy + 1 < p.dy && gx >= 1 && gx + 1 < p.dx) {
+            // no wrap: only the sources across a wall layer (z = 3 or dz - 4) are solid
+            const bool loA = gz == 3, hiA = gz == p.dz - 4, loB = gz + 1 == 3, hiB = gz + 1 == p.dz - 4;
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const unsigned src = I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q));
+                const bool sA = (cz(q) == 1 && loA) || (cz(q) == -1 && hiA);
+                const bool sB = (cz(q) == 1 && loB) || (cz(q) == -1 && hiB);
+                hv[q - 1] = SP::make(inA ? *(sA ? slot(q - 1, I) : slot(opp(q) - 1, src)) : SP::zero(),
+                                     inB ? *(sB ? slot(q - 1, I + 1) : slot(opp(q) - 1, src + 1)) : SP::zero());
+            }
+        } else {
+#pragma unroll
+            for (int q = 1; q < Q; ++q)
+                hv[q - 1] = SP::make(inA ? load_general(q, gx, gz, I) : SP::zero(),
+                                     inB ? load_general(q, gx, gz + 1, I + 1) : SP::zero());
+        }
+    };
+
+    // force on one node from the (rho, mu) ring, centre index c
+    auto force = [&](const float2 *const pl[7], int c, float &r, float gr[3], float F[3]) {
+        float2 g0 = make_float2(0.f, 0.f), g1 = g0, g2 = g0;
+        auto line = [&](int sx, int sy, int sz) -> float2 {
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int d = 1; d <= 3; ++d) {
+                const float k = d == 1 ? 45.f : (d == 2 ? -9.f : 1.f);
+                const int mo = sy * d * MZ + sz * d;
+                const float2 a = pl[3 + sx * d][c + mo], b = pl[3 - sx * d][c - mo];
+                acc = __ffma2_rn(make_float2(k, k), __fadd2_rn(a, make_float2(-b.x, -b.y)), acc);
+            }
+            return acc;
+        };
+        const float2 two = make_float2(2.f, 2.f);
+        float2 l;
+        l = line(1, 0, 0); g0 = __ffma2_rn(two, l, g0);
+        l = line(0, 1, 0); g1 = __ffma2_rn(two, l, g1);
+        l = line(0, 0, 1); g2 = __ffma2_rn(two, l, g2);
+        l = line(1, 1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, l);
+        l = line(1, -1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, make_float2(-l.x, -l.y));
+        l = line(1, 0, 1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, l);
+        l = line(1, 0, -1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
+        l = line(0, 1, 1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, l);
+        l = line(0, 1, -1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
+        const float inv360 = 1.0f / 360.0f;
+        const float gm[3] = {g0.y * inv360, g1.y * inv360, g2.y * inv360};
+        gr[0] = g0.x * inv360;
+        gr[1] = g1.x * inv360;
+        gr[2] = g2.x * inv360;
+        r = pl[3][c].x;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) F[a] = fmaf(-gm[a], r, gr[a] * (1.0f / 3.0f));
+    };
+
+    // prologue: as fused_tile
+    T hv[Q - 1];
+    for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) issue_rho(x);
+    issue_f0(x0 - 1);
+    issue_f0(x0);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    comp_mu(x0 - 3);
+    for (int x = x0 - 2; x <= x0 + 2; ++x) {
+        __syncthreads();
+        issue_rho(x + L);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        comp_mu(x);
+    }
+    __syncthreads();
+    issue_rho(x0 + 3 + L);
+    issue_f0(x0 + 1);
+    cp_async_commit();
+    fetch(x0, hv);
+
+    const int mc = (ty + 3) * MZ + (tz + 3);
+    const int ac = (ty + 1) * AZ + (tz + 2);  // even
+    for (int x = x0; x < x1; ++x) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (x + 1 < x1) {
+            issue_rho(x + 4 + L);
+            issue_f0(x + 2);
+        }
+        cp_async_commit();
+        T hn[Q - 1];
+        if (x + 1 < x1) fetch(x + 1, hn);
+        comp_mu(x + 3);
+        __syncthreads();
+        if (any) {
+            const float2 *pl[7];
+#pragma unroll
+            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + ((x + d) & 7) * (MY * MZ);
+            float rA, rB, grA[3], grB[3], FA[3], FB[3];
+            force(pl, mc, rA, grA, FA);
+            force(pl, mc + 1, rB, grB, FB);
+            const float2 r = make_float2(rA, rB);
+
+            const float *fa[3];
+            fa[0] = sf0 + ((x - 1) & 3) * (AY * AZ);
+            fa[1] = sf0 + (x & 3) * (AY * AZ);
+            fa[2] = sf0 + ((x + 1) & 3) * (AY * AZ);
+            const float2 a0 = *reinterpret_cast<const float2 *>(fa[1] + ac);
+            float2 f[Q];
+            f[0] = a0;
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const float *src = fa[1 - cx(q)] + ac - cy(q) * AZ - cz(q);
+                float2 a;
+                if (yz_fast || p.wall_mode != 1) {
+                    a = (cz(q) & 1) ? make_float2(src[0], src[1]) : *reinterpret_cast<const float2 *>(src);
+                } else {
+                    const int skA = gz - cz(q), skB = gz + 1 - cz(q);
+                    a.x = (skA < 3 || skA > p.dz - 4) ? a0.x : src[0];
+                    a.y = (skB < 3 || skB > p.dz - 4) ? a0.y : src[1];
+                }
+                f[q] = fma(K(wgt<float>(q)), SP::tof(hv[q - 1]), mul(K(ratio0(q)), a));
+            }
+            const float2 ir = make_float2(1.0f / r.x, 1.0f / r.y);
+            const float2 ux = mul(sub(sub(sub(sub(sub(add(add(add(add(f[1], f[7]), f[9]), f[11]), f[13]), f[2]), f[8]),
+                                              f[10]), f[12]), f[14]), ir);
+            const float2 uy = mul(sub(sub(sub(sub(sub(add(add(add(add(f[3], f[7]), f[8]), f[15]), f[17]), f[4]), f[9]),
+                                              f[10]), f[16]), f[18]), ir);
+            const float2 uz = mul(sub(sub(sub(sub(sub(add(add(add(add(f[5], f[11]), f[12]), f[15]), f[16]), f[6]),
+                                                  f[13]), f[14]), f[17]), f[18]), ir);
+            const float2 Fx = make_float2(FA[0], FB[0]), Fy = make_float2(FA[1], FB[1]), Fz = make_float2(FA[2], FB[2]);
+            if (p.qp) {
+                float qa[Q], qb[Q];
+#pragma unroll
+                for (int a = 0; a < Q; ++a) qa[a] = qb[a] = 0.f;
+                auto fill = [&](const float gr[3], float qp[Q]) {
+                    qp[1] = -19.f * (p.k1 + 3.f * p.k2) * (gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+                    qp[9] = -p.k1 * (2.f * gr[0] * gr[0] - gr[1] * gr[1] - gr[2] * gr[2]);
+                    qp[11] = -p.k1 * (gr[1] * gr[1] - gr[2] * gr[2]);
+                    qp[13] = -p.k1 * gr[0] * gr[1];
+                    qp[14] = -p.k1 * gr[2] * gr[1];
+                    qp[15] = -p.k1 * gr[0] * gr[2];
+                };
+                fill(grA, qa);
+                fill(grB, qb);
+                float2 qp2[Q];
+#pragma unroll
+                for (int a = 0; a < Q; ++a) qp2[a] = make_float2(qa[a], qb[a]);
+                collide_mrt_edm_fused2(f, r, ir, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, qp2);
+            } else {
+                collide_mrt_edm_fused2(f, r, ir, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, nullptr);
+            }
+
+            // encode against the pair's new rest populations and stream
+            const int gx = wrap_small(x, p.dx);
+            const unsigned I = (unsigned)gx * plane + (unsigned)(gy * p.dz + gz);
+            const float2 an = f[0];
+            if (ev && both) {
+                *reinterpret_cast<float2 *>(f0n + I) = an;
+            } else {
+                if (inA) f0n[I] = an.x;
+                if (inB) f0n[I + 1] = an.y;
+            }
+            if (P == 0 && ev && both) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q)
+                    *reinterpret_cast<T *>(slot(opp(q) - 1, I)) =
+                        SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+            } else if (P == 0) {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const T v = SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+                    if (inA) *slot(opp(q) - 1, I) = SP::lo(v);
+                    if (inB) *slot(opp(q) - 1, I + 1) = SP::hi(v);
+                }
+            } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
+                if (ev) {
+#pragma unroll
+                    for (int q = 1; q < Q; ++q) {
+                        const T v = SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+                        S *ptr = slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
+                        if (cz(q) & 1) {
+                            ptr[0] = SP::lo(v);
+                            ptr[1] = SP::hi(v);
+                        } else {
+                            *reinterpret_cast<T *>(ptr) = v;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 1; q < Q; ++q) {
+                        const T v = SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+                        S *ptr = slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)));
+                        ptr[0] = SP::lo(v);
+                        ptr[1] = SP::hi(v);
+                    }
+                }
+            } else if (p.wall_mode == 1 && gy >= 1 && gy + 1 < p.dy && gx >= 1 && gx + 1 < p.dx) {
+                const bool loA = gz == 3, hiA = gz == p.dz - 4, loB = gz + 1 == 3, hiB = gz + 1 == p.dz - 4;
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const T v = SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+                    const unsigned dst = I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q));
+                    const bool sA = (cz(q) == -1 && loA) || (cz(q) == 1 && hiA);
+                    const bool sB = (cz(q) == -1 && loB) || (cz(q) == 1 && hiB);
+                    if (inA) *(sA ? slot(opp(q) - 1, I) : slot(q - 1, dst)) = SP::lo(v);
+                    if (inB) *(sB ? slot(opp(q) - 1, I + 1) : slot(q - 1, dst + 1)) = SP::hi(v);
+                }
+            } else {
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const T v = SP::fromf(mul(fma(K(-ratio0(q)), an, f[q]), K(inv_w(q))));
+                    if (inA) store_general(q, gx, gz, I, SP::lo(v));
+                    if (inB) store_general(q, gx, gz + 1, I + 1, SP::hi(v));
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < Q - 1; ++q) hv[q] = hn[q];
+    }
+    cp_async_wait_all();
+}
+
+// Registers: at most 128 per thread for 4-byte storage pairs and the
+// half-precision ones alike (two CTAs of 256 threads per SM).
+template <int NT>
+constexpr int fused2_min_blocks()
+{
+    return NT >= 512 ? 1 : 512 / NT;
+}
+
+template <class S, int TY, int TZ, int L>
+__global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
+    k_fused2_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
+                     float *__restrict__ f0n, const float *__restrict__ rho, int xl)
+{
+    extern __shared__ float4 smem4[];
+    fused_tile2<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl, smem4);
+}
+
+// Persistent batch form (see k_fused_collide_batch).
+template <class S, int TY, int TZ, int L>
+__global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
+    k_fused2_collide_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
+                           int nbox, long long total_items, int P, int xl, unsigned int *counter)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ long long item_s;
+    __shared__ int box_s;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = (long long)atomicAdd(counter, 1u);
+            int lo = 0, hi = nbox - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) / 2;
+                if (boxes[mid].item0 <= it) lo = mid;
+                else hi = mid - 1;
+            }
+            item_s = it;
+            box_s = lo;
+        }
+        __syncthreads();
+        const long long it = item_s;
+        if (it >= total_items) break;
+        const BatchBox &bx = boxes[box_s];
+        const KParams<float> &p = params[box_s];
+        const long long local = it - bx.item0;
+        const int per_chunk = bx.tiles_z * bx.tiles_y;
+        const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
+        const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
+        fused_tile2<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ, ytile * TY,
+                                  chunk * xl, xl, smem4);
+        __syncthreads();
+    }
+}
+
+}  // namespace cpmp

@@ -1,0 +1,143 @@
+// k_fused2_impl.cuh -- launchers of the paired FUSED collide for one storage
+// type; each k_fused2_<storage>.cu instantiates them for its type so the
+// three compile in parallel.
+#pragma once
+
+#include "k_fused2.cuh"
+#include "kernels.h"
+
+namespace cpmp {
+namespace fused2_detail {
+
+template <class S, int TY, int TZ, int L>
+constexpr size_t smem2() { return FusedGeom2<TY, TZ, L>::BYTES; }
+
+template <class S, int TY, int TZ, int L>
+void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, float *f0n, const float *rho,
+              cudaStream_t st)
+{
+    const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + xl - 1) / xl);
+    constexpr int nt = TY * TZ / 2;
+    k_fused2_collide<S, TY, TZ, L><<<grid, nt, smem2<S, TY, TZ, L>(), st>>>(p, P, h, f0c, f0n, rho, xl);
+}
+
+template <class S, int TY, int TZ, int L>
+void batch_t(const KParams<float> *params, const BatchBox *boxes, int nbox, long long total, int P, int xl,
+             unsigned *counter, cudaStream_t st)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    constexpr int nt = TY * TZ / 2;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused2_collide_batch<S, TY, TZ, L>, nt,
+                                                  smem2<S, TY, TZ, L>());
+    long long grid = (long long)sms * (per_sm > 1 ? per_sm : 1);
+    if (grid > total) grid = total;
+    if (grid < 1) grid = 1;
+    k_fused2_collide_batch<S, TY, TZ, L><<<(unsigned)grid, nt, smem2<S, TY, TZ, L>(), st>>>(params, boxes, nbox,
+                                                                                           total, P, xl, counter);
+}
+
+template <class S, int TY, int TZ, int L>
+bool set_attr_t(int max_smem)
+{
+    const size_t b = smem2<S, TY, TZ, L>();
+    if ((int)b > max_smem) return false;
+    const bool ok =
+        cudaFuncSetAttribute(k_fused2_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)b) == cudaSuccess &&
+        cudaFuncSetAttribute(k_fused2_collide_batch<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)b) == cudaSuccess;
+    cudaGetLastError();
+    return ok;
+}
+
+// the paired tile shapes (nodes): 8x32, 16x32, 8x64
+template <class S, int L, class F>
+bool by_shape(int ty, int tz, F f)
+{
+    if (ty == 8 && tz == 32) return f.template operator()<S, 8, 32, L>();
+    if (ty == 16 && tz == 32) return f.template operator()<S, 16, 32, L>();
+    if (ty == 8 && tz == 64) return f.template operator()<S, 8, 64, L>();
+    return false;
+}
+
+struct SetAttr {
+    int max_smem;
+    template <class S, int TY, int TZ, int L>
+    bool operator()() { return set_attr_t<S, TY, TZ, L>(max_smem); }
+};
+struct Launch {
+    const KParams<float> *p;
+    int P, xl;
+    void *h;
+    const float *f0c;
+    float *f0n;
+    const float *rho;
+    cudaStream_t st;
+    template <class S, int TY, int TZ, int L>
+    bool operator()()
+    {
+        launch_t<S, TY, TZ, L>(*p, P, xl, (S *)h, f0c, f0n, rho, st);
+        return true;
+    }
+};
+struct Batch {
+    const KParams<float> *params;
+    const BatchBox *boxes;
+    int nbox;
+    long long total;
+    int P, xl;
+    unsigned *counter;
+    cudaStream_t st;
+    template <class S, int TY, int TZ, int L>
+    bool operator()()
+    {
+        batch_t<S, TY, TZ, L>(params, boxes, nbox, total, P, xl, counter, st);
+        return true;
+    }
+};
+
+template <class S>
+bool set_attr(int lap_order, int ty, int tz, int max_smem)
+{
+    SetAttr f{max_smem};
+    return lap_order == 7 ? by_shape<S, 3>(ty, tz, f) : by_shape<S, 2>(ty, tz, f);
+}
+template <class S>
+bool launch(const KParams<float> &p, int P, const FusedTile &t, void *h, const float *f0c, float *f0n,
+            const float *rho, cudaStream_t st)
+{
+    Launch f{&p, P, t.xl, h, f0c, f0n, rho, st};
+    return p.lap_order == 7 ? by_shape<S, 3>(t.ty, t.tz, f) : by_shape<S, 2>(t.ty, t.tz, f);
+}
+template <class S>
+bool batch(int lap_order, const FusedTile &t, const KParams<float> *params, const BatchBox *boxes, int nbox,
+           long long total, int P, unsigned *counter, cudaStream_t st)
+{
+    Batch f{params, boxes, nbox, total, P, t.xl, counter, st};
+    return lap_order == 7 ? by_shape<S, 3>(t.ty, t.tz, f) : by_shape<S, 2>(t.ty, t.tz, f);
+}
+
+}  // namespace fused2_detail
+}  // namespace cpmp
+
+// Defines the storage's three entry points (declared in kernels.h).
+#define CPMP_FUSED2_UNIT(SUFFIX, STYPE)                                                                          \
+    namespace cpmp {                                                                                             \
+    bool fused2_set_attr_##SUFFIX(int lap_order, int ty, int tz, int max_smem)                                   \
+    {                                                                                                            \
+        return fused2_detail::set_attr<STYPE>(lap_order, ty, tz, max_smem);                                     \
+    }                                                                                                            \
+    bool fused2_launch_##SUFFIX(const KParams<float> &p, int P, const FusedTile &t, void *h, const float *f0c,   \
+                                float *f0n, const float *rho, cudaStream_t st)                                   \
+    {                                                                                                            \
+        return fused2_detail::launch<STYPE>(p, P, t, h, f0c, f0n, rho, st);                                      \
+    }                                                                                                            \
+    bool fused2_batch_##SUFFIX(int lap_order, const FusedTile &t, const KParams<float> *params,                  \
+                               const BatchBox *boxes, int nbox, long long total, int P, unsigned *counter,       \
+                               cudaStream_t st)                                                                  \
+    {                                                                                                            \
+        return fused2_detail::batch<STYPE>(lap_order, t, params, boxes, nbox, total, P, counter, st);            \
+    }                                                                                                            \
+    }

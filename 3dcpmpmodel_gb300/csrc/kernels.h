@@ -47,16 +47,32 @@ extern template void plain_launch_mu_force<double>(const KParams<double> &, cons
 
 // ---- FUSED scheme (k_fused.cu) --------------------------------------------
 // storage: CPMP_STORE_F32 / F16 / BF16
+// ty x tz nodes per CTA, an x march of xl planes, np nodes per thread (1, or
+// 2 for the paired kernel of k_fused2.cu)
 struct FusedTile {
     int ty, tz, xl;
+    int np = 1;
 };
 // Tile shapes instantiated for the fused kernel; the autotuner picks among
 // them per grid.
 int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
-bool fused_tile_supported(int ty, int tz);
+bool fused_tile_supported(int ty, int tz, int np = 1);
 // The (storage, Laplacian, tile) instantiation fits this device's shared memory.
-bool fused_tile_usable(int storage, int lap_order, int ty, int tz);
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1);
+// Paired kernel (k_fused2_<storage>.cu, one unit per storage type): each
+// returns false when (ty, tz) is not one of its shapes.
+#define CPMP_FUSED2_DECL(SUFFIX)                                                                                 \
+    bool fused2_set_attr_##SUFFIX(int lap_order, int ty, int tz, int max_smem);                                  \
+    bool fused2_launch_##SUFFIX(const KParams<float> &p, int P, const FusedTile &t, void *h, const float *f0c,   \
+                                float *f0n, const float *rho, cudaStream_t st);                                  \
+    bool fused2_batch_##SUFFIX(int lap_order, const FusedTile &t, const KParams<float> *params,                  \
+                               const BatchBox *boxes, int nbox, long long total, int P, unsigned *counter,       \
+                               cudaStream_t st);
+CPMP_FUSED2_DECL(f16)
+CPMP_FUSED2_DECL(bf16)
+CPMP_FUSED2_DECL(f32)
+#undef CPMP_FUSED2_DECL
 
 cudaError_t fused_setup_attributes();
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
@@ -75,7 +91,7 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 // pass.  params/boxes are device arrays of nbox entries; counter is one
 // device unsigned (reset here); max_dx / max_cols bound the boxes' x extent
 // and wall columns, max_pairs the density pass's node pairs per x plane
-// (dy * (dz / 2 + 1)).
+// (dy * ((dz + 1) / 2)).
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
                       int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter, cudaStream_t st,

@@ -103,9 +103,10 @@ __device__ __forceinline__ R mu0(int eos, R A, R B, R T, R rho)
 }
 
 // Single-precision mu0 for the fused kernel: the same expressions with the
-// per-launch constants hoisted, one reciprocal per distinct denominator and
-// the hardware log2 (__logf: absolute error 2^-21.4 near 1, 3 ulp elsewhere;
-// mu is a sum of O(0.1) terms, so this stays at FP32 rounding level).
+// per-launch constants hoisted, one reciprocal per distinct denominator
+// (__fdividef: 2 ulp) and the hardware log2 (__logf: absolute error 2^-21.4
+// near 1, 3 ulp elsewhere); mu is a sum of O(0.1) terms, so this stays at
+// FP32 rounding level.
 #ifdef __CUDACC__
 struct EosFast {
     int eos;
@@ -124,17 +125,17 @@ __device__ __forceinline__ float mu0_fast(const EosFast &e, float rho)
     float d = rho;
     if (d > R0) d = R0 + __fdividef(d - R0, 1.0f + (d - R0) * W0);
     const float bd = e.B * d;
-    const float ir = __frcp_rn(1.0f - bd);
+    const float ir = __fdividef(1.0f, 1.0f - bd);
     if (e.eos == 2) {
         const float om3 = ir * ir * ir;
         return e.T * __logf(d) + e.T + e.T * (8.f * bd - 9.f * bd * bd + 3.f * bd * bd * bd) * om3 - 2.f * e.A * d;
     }
     const float base = e.T * __logf(d * ir) + e.T * ir;
     if (e.eos == 1) return base - 2.f * e.A * d;
-    if (e.eos == 3) return base - e.c_att * __logf(1.0f + bd) - e.A * d * __frcp_rn(1.0f + bd);
+    if (e.eos == 3) return base - e.c_att * __logf(1.0f + bd) - e.A * d * __fdividef(1.0f, 1.0f + bd);
     const float s2 = 1.41421356237f;
-    return base - e.c_att * __logf((s2 - 1.0f + bd) * __frcp_rn(s2 + 1.0f - bd)) -
-           e.A * d * __frcp_rn(1.0f + bd * 2.0f - bd * bd);
+    return base - e.c_att * __logf((s2 - 1.0f + bd) * __fdividef(1.0f, s2 + 1.0f - bd)) -
+           e.A * d * __fdividef(1.0f, 1.0f + bd * 2.0f - bd * bd);
 }
 #endif  // __CUDACC__
 

@@ -217,6 +217,12 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
  * length explicitly (no reference counterpart).  CPMP_ERR_UNSUPPORTED when the
  * tile is not instantiated or does not fit the device's shared memory. */
 cpmp_status cpmp_set_tile(cpmp_handle *h, int tile_y, int tile_z, int march_x);
+/* As cpmp_set_tile with the nodes each thread owns: 1, or 2 for the paired
+ * kernel (two z-adjacent nodes per thread, paired FP32 instructions; same
+ * results bit for bit).  cpmp_set_tile is nodes_per_thread = 1. */
+cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread);
+/* The tile in use (after cpmp_autotune: the one it kept).  Outputs may be NULL. */
+cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread);
 
 /* The CUDA stream the handle launches on (cudaStream_t). */
 void *cpmp_stream(cpmp_handle *h);
@@ -306,6 +312,8 @@ cpmp_status cpmp_batch_sync(cpmp_batch *b);
 /* Tile shape / x-march shared by all boxes; the autotuner times the
  * candidates on scratch copies of every box (the state is not advanced). */
 cpmp_status cpmp_batch_set_tile(cpmp_batch *b, int tile_y, int tile_z, int march_x);
+cpmp_status cpmp_batch_set_tile_ex(cpmp_batch *b, int tile_y, int tile_z, int march_x, int nodes_per_thread);
+cpmp_status cpmp_batch_get_tile(cpmp_batch *b, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread);
 cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *march_x, double *ms_per_step);
 cpmp_status cpmp_batch_set_kernel_timing(cpmp_batch *b, int on);
 int cpmp_batch_kernel_times(cpmp_batch *b, const char **names, long long *launches, double *ms, int cap);

@@ -178,12 +178,38 @@ def test_fused_result_is_independent_of_tile(cpmp, storage):
     the same decode and summation order, so any tile gives the same bits."""
     cfg = dict(dx=48, dy=24, dz=40, radius=9.0, width=4.0, base_pt=-0.04)
     runs = []
-    for ty, tz, xl in ((8, 32, 16), (4, 32, 7), (1, 128, 48), (2, 64, 5)):
+    for ty, tz, xl, npt in ((8, 32, 16, 1), (4, 32, 7, 1), (1, 128, 48, 1), (2, 64, 5, 1), (8, 32, 16, 2),
+                            (16, 32, 7, 2), (8, 64, 48, 2)):
         s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
-        s.set_tile(ty, tz, xl)
+        s.set_tile(ty, tz, xl, npt)
         s.step(12)
         runs.append((s.get("rho"), s.get("dist")))
         s.close()
+    for r, d in runs[1:]:
+        assert np.array_equal(r, runs[0][0])
+        assert np.array_equal(d, runs[0][1])
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(dx=20, dy=18, dz=37, radius=7.0, width=4.0, base_pt=-0.04),                      # odd DZ, walls
+    dict(dx=24, dy=20, dz=30, radius=6.0, width=3.0, wall_mode=0, centre=(12, 10, 15)),   # periodic
+    dict(dx=20, dy=18, dz=26, radius=6.0, width=4.0, base_pt=0.02, K1=0.002, K2=-0.002, tau=1.0,
+         lap_order=7),                                                                    # K1/K2, 7-point
+], ids=["odd_dz", "periodic", "k1k2_lap7"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f32"])
+def test_paired_kernel_matches_single_node_kernel(cpmp, cfg, storage):
+    """Two nodes per thread (paired FP32 instructions) give exactly the bits
+    of one node per thread, on every global-access path: odd DZ (no paired
+    accesses), periodic edges, walls, the K1/K2 term and the 7-point
+    Laplacian."""
+    runs = []
+    for ty, tz, xl, npt in ((8, 32, 9, 1), (8, 32, 9, 2), (16, 32, 5, 2), (8, 64, 64, 2)):
+        s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
+        s.set_tile(ty, tz, xl, npt)
+        s.step(11)
+        runs.append((s.get("rho"), s.get("dist")))
+        s.close()
+    assert np.isfinite(runs[0][0]).all() and np.isfinite(runs[0][1]).all()
     for r, d in runs[1:]:
         assert np.array_equal(r, runs[0][0])
         assert np.array_equal(d, runs[0][1])
