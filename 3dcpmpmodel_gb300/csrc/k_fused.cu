@@ -131,8 +131,10 @@ void launch_collide_t(const KParams<float> &p, int P, const FusedTile &t, S *h, 
                       float *f0n, const float *rho, cudaStream_t st)
 {
     const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + t.xl - 1) / t.xl);
+    SlotTable<S> slots;
+    for (int k = 0; k < Q - 1; ++k) slots.q[k] = h + (size_t)p.n * k;
     k_fused_collide<S, TY, TZ, L><<<grid, TY * TZ, fused_smem_bytes<S, TY, TZ, L>(), st>>>(
-        p, P, h, f0c, f0n, rho, t.xl);
+        p, P, slots, f0c, f0n, rho, t.xl);
 }
 
 template <class S, int L>
@@ -309,8 +311,8 @@ void batch_collide_l(const FusedTile &t, const KParams<float> *params, const Bat
 
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter, cudaStream_t st,
-                      LaunchHook *hook)
+                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter,
+                      cudaStream_t st, LaunchHook *hook)
 {
     if (wall_mode == 1) {
         const dim3 gw((unsigned)((max_cols + 127) / 128), (unsigned)nbox);

@@ -201,18 +201,56 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
     *reinterpret_cast<float2 *>(rho + I) = r;
 }
 
+// Density of one fluid node k of an x/y-interior column of a walled box
+// (wall_mode 1): the paired path's sums (r += w_q h_q, then r += (w_q / w_0)
+// a_q, q in order, fused multiply-adds) with each source across the wall
+// layer (k = 3 or dz - 4) replaced by the node's own slot and rest population.
+template <class S>
+__device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P, const S *__restrict__ h,
+                                                  const float *__restrict__ f0, float *__restrict__ rho,
+                                                  unsigned I, int k)
+{
+    const unsigned n = (unsigned)p.n;
+    const int plane = p.dy * p.dz;
+    const bool lo = k == 3, hi = k == p.dz - 4;
+    const float a0 = f0[I];
+    float hv[Q - 1], a[Q - 1];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        const unsigned src = I - (unsigned)(cx(q) * plane + cy(q) * p.dz + cz(q));
+        const bool ss = (cz(q) == 1 && lo) || (cz(q) == -1 && hi);
+        const size_t hi_idx = (P == 0 || ss) ? (size_t)n * (unsigned)(q - 1) + I : (size_t)n * (unsigned)(opp(q) - 1) + src;
+        hv[q - 1] = s2f<S>(h[hi_idx]);
+        a[q - 1] = ss ? a0 : f0[src];
+    }
+    float r = a0;
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        r = fmaf(wgt<float>(q), hv[q - 1], r);
+        r = fmaf(ratio0(q), a[q - 1], r);
+    }
+    rho[I] = r;
+}
+
 // Density of the nodes k0 and k0 + 1 of column (i, j) (either may lie
 // outside [0, dz)); the node index of k0 is even (see pair_k0).  Pairs next
-// to a wall or a periodic edge take the general per-node path.
+// to a z wall in an x/y-interior column take density_wall_node, pairs at a
+// periodic edge the general per-node path.
 template <class S>
 __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, const S *__restrict__ h,
                                              const float *__restrict__ f0, float *__restrict__ rho, int i, int j,
                                              int k0)
 {
     const bool in0 = k0 >= 0 && k0 < p.dz, in1 = k0 + 1 >= 0 && k0 + 1 < p.dz;
-    const bool fast = in0 && in1 && i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy && z_plain(p, k0) &&
-                      z_plain(p, k0 + 1);
+    const bool xy = i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy;
+    const bool fast = in0 && in1 && xy && z_plain(p, k0) && z_plain(p, k0 + 1);
     if (!fast) {
+        const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
+        if (xy && p.wall_mode == 1) {
+            if (in0 && !solid_k(1, k0, p.dz)) density_wall_node<S>(p, P, h, f0, rho, I, k0);
+            if (in1 && !solid_k(1, k0 + 1, p.dz)) density_wall_node<S>(p, P, h, f0, rho, I + 1, k0 + 1);
+            return;
+        }
         if (in0) density_node<S>(p, P, h, f0, rho, i, j, k0);
         if (in1) density_node<S>(p, P, h, f0, rho, i, j, k0 + 1);
         return;
@@ -275,9 +313,14 @@ struct FusedGeom {
     static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
     static constexpr int RM_PAIRS = 8 * MY * MZ;     // (rho, mu) planes x-3 .. x+3 (+1 being written)
     static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
-    static constexpr int TAB_INTS = 2 * RY + RZ;
+    // per-tile element tables: (centre in the rho plane | solid flag, wall
+    // offset) of each (rho, mu) element; plane offsets of the rho and anchor
+    // ring elements; wrapped y, z rows
+    static constexpr int MTAB_INT2 = MY * MZ;
+    static constexpr int TAB_INTS = 2 * RY + RZ + RY * RZ + AY * AZ;
     static constexpr size_t BASE_BYTES = sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
-                                         sizeof(float) * F0_FLOATS + sizeof(int) * TAB_INTS;
+                                         sizeof(float) * F0_FLOATS + sizeof(int2) * MTAB_INT2 +
+                                         sizeof(int) * TAB_INTS;
     template <class S>
     static constexpr size_t bytes()
     {
@@ -293,6 +336,22 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
+// addressing): as base pointers in the launch's parameter space, so that an
+// access is one multiply-add on a constant operand, or as h + n k (the items
+// of a batch, whose boxes differ).
+template <class S>
+struct SlotTable {
+    S *q[Q - 1];
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
+};
+template <class S>
+struct SlotBase {
+    S *h;
+    unsigned n;
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return h + (size_t)n * (unsigned)k + idx; }
+};
+
 // One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
 // x.  Shared-memory rings:
 //   rho : planes x+3-L .. x+4+L, halo 3+L (L = 2: five-point Laplacian, 3: seven-point)
@@ -305,8 +364,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // solid nodes), then every fluid node of plane x computes
 // F = -rho grad7(mu) + grad7(rho)/3, decodes its populations, collides (MRT +
 // exact-difference forcing) and streams A-A in place.
-template <class S, int TY, int TZ, int L>
-__device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__restrict__ h,
+template <class S, int TY, int TZ, int L, class SL>
+__device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const SL &slots,
                                            const float *__restrict__ f0c, float *__restrict__ f0n,
                                            const float *__restrict__ rho, const int z0, const int y0,
                                            const int x0, const int xl, float4 *smem4)
@@ -318,21 +377,23 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
     float *srho = reinterpret_cast<float *>(smem4);
     float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
     float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
-    int *tabY = reinterpret_cast<int *>(sf0 + G::F0_FLOATS);
+    int2 *mtab = reinterpret_cast<int2 *>(sf0 + G::F0_FLOATS);
+    int *tabY = reinterpret_cast<int *>(mtab + G::MTAB_INT2);
     int *tabZ = tabY + RY;
     int *tabYdz = tabZ + RZ;  // wrapped y row times dz
+    int *offR = tabYdz + RY;  // rho ring element -> offset in its x plane
+    int *offA = offR + RY * RZ;  // anchor ring element -> offset in its x plane
 
     const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
     const int x1 = min(x0 + xl, p.dx);
-    // node indices are 32-bit (the FUSED scheme keeps N below 2^32); slot q of
-    // node I is h + q * n + I with a 64-bit product
+    // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
     const unsigned plane = (unsigned)(p.dy * p.dz);
-    const unsigned n = (unsigned)p.n;
-    auto slot = [&](int q, unsigned idx) -> S * { return h + (size_t)n * (unsigned)q + idx; };
+    auto slot = [&](int q, unsigned idx) -> S * { return slots(q, idx); };
     const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
     const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
 
-    // wrapped y / z coordinates of the halo rows and columns
+    // wrapped y / z coordinates of the halo rows and columns, then the
+    // element tables the per-plane loops read (fixed for the whole march)
     for (int e = threadIdx.x; e < RY + RZ; e += NT) {
         if (e < RY) {
             tabY[e] = wrap_small(y0 - RH + e, p.dy);
@@ -342,21 +403,40 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
         }
     }
     __syncthreads();
+    for (int e = threadIdx.x; e < RY * RZ; e += NT) {
+        const int ly = e / RZ, lz = e - ly * RZ;
+        offR[e] = tabYdz[ly] + tabZ[lz];
+    }
+    for (int e = threadIdx.x; e < AY * AZ; e += NT) {
+        const int ly = e / AZ, lz = e - ly * AZ;
+        offA[e] = tabYdz[ly + RH - 1] + tabZ[lz + RH - 1];
+    }
+    for (int e = threadIdx.x; e < MY * MZ; e += NT) {
+        const int my = e / MZ, mz = e - my * MZ;
+        const int c = (my + L) * RZ + (mz + L), gz = tabZ[mz + L];
+        const int woff = (gz < 3 ? 0 : p.dx * p.dy) + tabY[my + L];
+        mtab[e] = make_int2(solid_k(p.wall_mode, gz, p.dz) ? (int)((unsigned)c | 0x80000000u) : c, woff);
+    }
+    __syncthreads();
 
+    // per-plane element loops: a fixed trip count, the last pass predicated
+    constexpr int KR = (RY * RZ + NT - 1) / NT, KA = (AY * AZ + NT - 1) / NT, KM = (MY * MZ + NT - 1) / NT;
     auto issue_rho = [&](int xlog) {
         const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = srho + (xlog & (NR - 1)) * (RY * RZ);
-        for (int e = threadIdx.x; e < RY * RZ; e += NT) {
-            const int ly = e / RZ, lz = e - ly * RZ;
-            cp_async4(dst + e, src + (unsigned)(tabYdz[ly] + tabZ[lz]));
+#pragma unroll
+        for (int k = 0; k < KR; ++k) {
+            const int e = threadIdx.x + k * NT;
+            if ((k + 1) * NT <= RY * RZ || e < RY * RZ) cp_async4(dst + e, src + (unsigned)offR[e]);
         }
     };
     auto issue_f0 = [&](int xlog) {
         const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = sf0 + (xlog & 3) * (AY * AZ);
-        for (int e = threadIdx.x; e < AY * AZ; e += NT) {
-            const int ly = e / AZ, lz = e - ly * AZ;
-            cp_async4(dst + e, src + (unsigned)(tabYdz[ly + RH - 1] + tabZ[lz + RH - 1]));
+#pragma unroll
+        for (int k = 0; k < KA; ++k) {
+            const int e = threadIdx.x + k * NT;
+            if ((k + 1) * NT <= AY * AZ || e < AY * AZ) cp_async4(dst + e, src + (unsigned)offA[e]);
         }
     };
     auto comp_mu = [&](int xlog) {
@@ -367,13 +447,16 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
         const float *rm2 = rpl(xlog - 2), *rp2 = rpl(xlog + 2);
         const float *rm3 = L == 3 ? rpl(xlog - 3) : rc;
         const float *rp3 = L == 3 ? rpl(xlog + 3) : rc;
-        for (int e = threadIdx.x; e < MY * MZ; e += NT) {
-            const int my = e / MZ, mz = e - my * MZ;
-            const int c = (my + L) * RZ + (mz + L);
+        const int wx = gx * p.dy;
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+            const int e = threadIdx.x + k * NT;
+            if (!((k + 1) * NT <= MY * MZ || e < MY * MZ)) break;
+            const int2 t = mtab[e];
+            const int c = t.x & 0x7fffffff;
             const float r0 = rc[c];
-            const int gz = tabZ[mz + L];
-            if (solid_k(p.wall_mode, gz, p.dz)) {
-                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : p.dx * p.dy) + gx * p.dy + tabY[my + L]]);
+            if (t.x < 0) {
+                dst[e] = make_float2(r0, p.wall[t.y + wx]);
                 continue;
             }
             float lap;
@@ -580,11 +663,11 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, S *__
 // One box: CTA (bx, by, bz) owns z tile bx, y tile by and x chunk bz.
 template <class S, int TY, int TZ, int L>
 __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
-    k_fused_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
+    k_fused_collide(KParams<float> p, int P, SlotTable<S> slots, const float *__restrict__ f0c,
                     float *__restrict__ f0n, const float *__restrict__ rho, int xl)
 {
     extern __shared__ float4 smem4[];
-    fused_tile<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
+    fused_tile<S, TY, TZ, L>(p, P, slots, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
                              smem4);
 }
 
@@ -620,15 +703,16 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ, ytile * TY,
-                                 chunk * xl, xl, smem4);
+        fused_tile<S, TY, TZ, L>(p, P, SlotBase<S>{(S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.f0[1 - P], bx.rho[P],
+                                 ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
         __syncthreads();
     }
 }
 
 // Batched density pass, one node pair per thread (the pairing of
 // k_density): blockIdx.z is the box, blockIdx.y the x plane, blockIdx.x the
-// plane's pairs in blocks of 128; blocks past a box's extent exit at once.
+// plane's pairs (numbered column by column) in blocks of 128; blocks past a
+// box's extent exit at once.
 template <class S>
 __global__ void __launch_bounds__(128) k_density_batch(const KParams<float> *__restrict__ params,
                                                        const BatchBox *__restrict__ boxes, int P)

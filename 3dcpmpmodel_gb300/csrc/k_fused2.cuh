@@ -74,8 +74,8 @@ struct FusedGeom2 {
 
 // One CTA owns a TY x TZ column tile and marches over xl planes of x; see
 // fused_tile for the rings and the order of work per plane.
-template <class S, int TY, int TZ, int L>
-__device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, S *__restrict__ h,
+template <class S, int TY, int TZ, int L, class SL>
+__device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, const SL &slots,
                                             const float *__restrict__ f0c, float *__restrict__ f0n,
                                             const float *__restrict__ rho, const int z0, const int y0,
                                             const int x0, const int xl, float4 *smem4)
@@ -97,8 +97,7 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, S *_
     const int tz = 2 * (threadIdx.x % TH), ty = threadIdx.x / TH;
     const int x1 = min(x0 + xl, p.dx);
     const unsigned plane = (unsigned)(p.dy * p.dz);
-    const unsigned n = (unsigned)p.n;
-    auto slot = [&](int q, unsigned idx) -> S * { return h + (size_t)n * (unsigned)q + idx; };
+    auto slot = [&](int q, unsigned idx) -> S * { return slots(q, idx); };
     const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
     const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
 
@@ -439,11 +438,12 @@ constexpr int fused2_min_blocks()
 
 template <class S, int TY, int TZ, int L>
 __global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
-    k_fused2_collide(KParams<float> p, int P, S *__restrict__ h, const float *__restrict__ f0c,
+    k_fused2_collide(KParams<float> p, int P, SlotTable<S> slots, const float *__restrict__ f0c,
                      float *__restrict__ f0n, const float *__restrict__ rho, int xl)
 {
     extern __shared__ float4 smem4[];
-    fused_tile2<S, TY, TZ, L>(p, P, h, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl, smem4);
+    fused_tile2<S, TY, TZ, L>(p, P, slots, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
+                              smem4);
 }
 
 // Persistent batch form (see k_fused_collide_batch).
@@ -476,8 +476,8 @@ __global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile2<S, TY, TZ, L>(p, P, (S *)bx.h, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ, ytile * TY,
-                                  chunk * xl, xl, smem4);
+        fused_tile2<S, TY, TZ, L>(p, P, SlotBase<S>{(S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.f0[1 - P],
+                                  bx.rho[P], ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
         __syncthreads();
     }
 }

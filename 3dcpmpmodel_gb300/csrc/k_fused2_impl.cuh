@@ -18,7 +18,9 @@ void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, fl
 {
     const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + xl - 1) / xl);
     constexpr int nt = TY * TZ / 2;
-    k_fused2_collide<S, TY, TZ, L><<<grid, nt, smem2<S, TY, TZ, L>(), st>>>(p, P, h, f0c, f0n, rho, xl);
+    SlotTable<S> slots;
+    for (int k = 0; k < Q - 1; ++k) slots.q[k] = h + (size_t)p.n * k;
+    k_fused2_collide<S, TY, TZ, L><<<grid, nt, smem2<S, TY, TZ, L>(), st>>>(p, P, slots, f0c, f0n, rho, xl);
 }
 
 template <class S, int TY, int TZ, int L>

@@ -94,8 +94,8 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 // (dy * ((dz + 1) / 2)).
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter, cudaStream_t st,
-                      LaunchHook *hook);
+                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter,
+                      cudaStream_t st, LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).
 void fused_launch_decode(int storage, const KParams<float> &p, int P, const void *h, const float *f0,
