@@ -338,18 +338,17 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
 // addressing): as base pointers in the launch's parameter space, so that an
-// access is one multiply-add on a constant operand, or as h + n k (the items
-// of a batch, whose boxes differ).
+// access is one multiply-add on a constant operand, or in shared memory (the
+// items of a batch, whose boxes differ).
 template <class S>
 struct SlotTable {
     S *q[Q - 1];
     __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
 };
 template <class S>
-struct SlotBase {
-    S *h;
-    unsigned n;
-    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return h + (size_t)n * (unsigned)k + idx; }
+struct SlotShared {
+    S *const *q;  // shared-memory copy of the item's box pointers
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
 };
 
 // One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
@@ -682,6 +681,7 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
     extern __shared__ float4 smem4[];
     __shared__ long long item_s;
     __shared__ int box_s;
+    __shared__ S *slot_s[Q - 1];
     for (;;) {
         if (threadIdx.x == 0) {
             const long long it = (long long)atomicAdd(counter, 1u);
@@ -699,12 +699,14 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
         if (it >= total_items) break;
         const BatchBox &bx = boxes[box_s];
         const KParams<float> &p = params[box_s];
+        // read first after the tile's own barriers
+        if (threadIdx.x < Q - 1) slot_s[threadIdx.x] = (S *)bx.h + (size_t)p.n * threadIdx.x;
         const long long local = it - bx.item0;
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile<S, TY, TZ, L>(p, P, SlotBase<S>{(S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.f0[1 - P], bx.rho[P],
-                                 ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
+        fused_tile<S, TY, TZ, L>(p, P, SlotShared<S>{slot_s}, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ,
+                                 ytile * TY, chunk * xl, xl, smem4);
         __syncthreads();
     }
 }

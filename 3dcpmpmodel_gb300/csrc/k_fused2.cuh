@@ -455,6 +455,7 @@ __global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
     extern __shared__ float4 smem4[];
     __shared__ long long item_s;
     __shared__ int box_s;
+    __shared__ S *slot_s[Q - 1];
     for (;;) {
         if (threadIdx.x == 0) {
             const long long it = (long long)atomicAdd(counter, 1u);
@@ -476,8 +477,9 @@ __global__ void __launch_bounds__(TY *TZ / 2, fused2_min_blocks<TY * TZ / 2>())
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile2<S, TY, TZ, L>(p, P, SlotBase<S>{(S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.f0[1 - P],
-                                  bx.rho[P], ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
+        if (threadIdx.x < Q - 1) slot_s[threadIdx.x] = (S *)bx.h + (size_t)p.n * threadIdx.x;
+        fused_tile2<S, TY, TZ, L>(p, P, SlotShared<S>{slot_s}, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ,
+                                  ytile * TY, chunk * xl, xl, smem4);
         __syncthreads();
     }
 }
