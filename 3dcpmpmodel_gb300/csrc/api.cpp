@@ -56,6 +56,11 @@ struct cpmp_handle {
     void *wall = nullptr;
     double *partials = nullptr, *dout = nullptr;
     double *impact_partials = nullptr;  // allocated by the first cpmp_impact_diag
+    // FUSED: max |MV|^2 of the last collision at each parity (float bits),
+    // sdiag[P * sdiag_stride]; a batch box points into its batch's array
+    unsigned *sdiag = nullptr;
+    int sdiag_stride = 1;
+    bool sdiag_owned = true;
     long long step = 0;
     bool initialised = false;
     std::unique_ptr<LaunchHook> hook;
@@ -76,6 +81,7 @@ struct cpmp_batch {
     KParams<float> *d_params = nullptr;
     BatchBox *d_boxes = nullptr;
     unsigned *d_counter = nullptr;
+    unsigned *d_mvmax = nullptr;  // [2][boxes]: each box's max |MV|^2 of its last collision, per parity
     long long total_items = 0, nodes = 0, max_cols = 0, max_pairs = 0, launches = 0;
     int max_dx = 0;
     cudaGraphExec_t gexec = nullptr;
@@ -112,6 +118,8 @@ KParams<R> make_kparams(const cpmp_handle *h)
         k.omts[q] = (R)(1.0 - h->ts[q]);
     }
     k.wall = (const R *)h->wall;
+    k.mvmax = h->sdiag;
+    k.mvmax_stride = h->sdiag_stride;
     return k;
 }
 
@@ -123,6 +131,8 @@ void free_all(cpmp_handle *h)
                     h->wall, h->partials, h->dout, h->impact_partials};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    if (h->sdiag && h->sdiag_owned) cudaFree(h->sdiag);
+    h->sdiag = nullptr;
     h->type = nullptr;
     h->rho = h->rho2 = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
     h->f0[0] = h->f0[1] = nullptr;
@@ -191,6 +201,7 @@ void launch_one_step(cpmp_handle *h, LaunchHook *hook)
     } else {
         auto k = make_kparams<float>(h);
         const int P = (int)(h->step & 1);
+        if (h->sdiag) cudaMemsetAsync(h->sdiag + P * h->sdiag_stride, 0, sizeof(unsigned), h->st);
         fused_launch_wall(k, (float *)h->rho, (float *)h->rho2, h->st, hook);
         fused_launch_collide(h->p.storage, k, P, h->tile, h->h, h->f0[P], h->f0[1 - P], (const float *)h->rho,
                              h->st, hook);
@@ -434,6 +445,10 @@ cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
     if ((s = dalloc((void **)&h->partials, 3 * sizeof(double) * diag_partial_blocks(h->n), "partials")) != CPMP_OK)
         return s;
     if ((s = dalloc((void **)&h->dout, 32 * sizeof(double), "dout")) != CPMP_OK) return s;
+    if (!h->plain) {
+        if ((s = dalloc((void **)&h->sdiag, 2 * sizeof(unsigned), "mv max")) != CPMP_OK) return s;
+        CK(cudaMemset(h->sdiag, 0, 2 * sizeof(unsigned)));
+    }
     if (h->plain) {
         if ((s = dalloc(&h->mu, n * rs, "mu")) != CPMP_OK) return s;
         if ((s = dalloc(&h->u, 3 * n * rs, "u")) != CPMP_OK) return s;
@@ -650,19 +665,31 @@ cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *
                                              (float *)h->rho, (float *)h->u, h->st);
         h->launches += 1;
     } else {
+        // page-locked host memory is read by the encode kernels in place;
+        // anything else goes through a device copy
+        cudaPointerAttributes at{};
+        const void *dsrc = nullptr;
+        if (cudaPointerGetAttributes(&at, src) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+            dsrc = at.devicePointer;
+        cudaGetLastError();
         void *tmp = nullptr;
-        cpmp_status s = dalloc(&tmp, CPMP_Q * n * es, "encode");
-        if (s != CPMP_OK) return s;
-        cudaError_t e = cudaMemcpyAsync(tmp, src, CPMP_Q * n * es, cudaMemcpyHostToDevice, h->st);
+        if (!dsrc) {
+            cpmp_status s = dalloc(&tmp, CPMP_Q * n * es, "encode");
+            if (s != CPMP_OK) return s;
+            dsrc = tmp;
+        }
+        for (int P = 0; P < 2; ++P)
+            if (h->sdiag) cudaMemsetAsync(h->sdiag + P * h->sdiag_stride, 0, sizeof(unsigned), h->st);
+        cudaError_t e = tmp ? cudaMemcpyAsync(tmp, src, CPMP_Q * n * es, cudaMemcpyHostToDevice, h->st) : cudaSuccess;
         const int P = (int)(h->step & 1);
         auto k = make_kparams<float>(h);
         if (e == cudaSuccess) {
-            fused_launch_encode(h->p.storage, k, P, h->h, h->f0[P], tmp, dtype == CPMP_F64, h->st);
+            fused_launch_encode(h->p.storage, k, P, h->h, h->f0[P], dsrc, dtype == CPMP_F64, h->st);
             fused_launch_density(h->p.storage, k, P, h->h, h->f0[P], (float *)h->rho, h->st, nullptr);
             h->launches += 3;
             e = cudaStreamSynchronize(h->st);
         }
-        cudaFree(tmp);
+        if (tmp) cudaFree(tmp);
         if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("encode: ") + cudaGetErrorString(e));
     }
     CK(cudaGetLastError());
@@ -675,13 +702,12 @@ cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
     if (!h || !out) return fail(CPMP_ERR_PARAM, "null argument");
     CK(cudaSetDevice(h->p.device));
     std::memset(out, 0, sizeof(*out));
-    if (!h->plain) {
-        cpmp_status s = fused_diag_fields(h);
-        if (s != CPMP_OK) return s;
-    }
+    // FUSED: max |MV| comes from the last collision (as the reference's MV
+    // array, written by its collide kernel); the mass pass reads rho only
+    const void *mv = h->plain ? h->mv : nullptr;
     const int tier = h->p.dy / 2;
     if (h->f64) {
-        diag_launch_mass<double>(h->type, (const double *)h->rho, (const double *)h->mv, h->n, h->partials,
+        diag_launch_mass<double>(h->type, (const double *)h->rho, (const double *)mv, h->n, h->partials,
                                  h->dout, h->st);
         if (h->p.dx >= 8 && h->p.dz >= 8)
             diag_launch_contact_angle<double>((const double *)h->rho, h->p.dx, h->p.dy, h->p.dz, tier, h->den_g,
@@ -689,7 +715,7 @@ cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
         diag_launch_laplace<double>((const double *)h->rho, h->p.dx, h->p.dy, h->p.dz, h->eos, h->A, h->B, h->T,
                                     h->p.k * h->p.k, h->dout + 12, h->st);
     } else {
-        diag_launch_mass<float>(h->type, (const float *)h->rho, (const float *)h->mv, h->n, h->partials, h->dout,
+        diag_launch_mass<float>(h->type, (const float *)h->rho, (const float *)mv, h->n, h->partials, h->dout,
                                 h->st);
         if (h->p.dx >= 8 && h->p.dz >= 8)
             diag_launch_contact_angle<float>((const float *)h->rho, h->p.dx, h->p.dy, h->p.dz, tier, h->den_g,
@@ -699,9 +725,18 @@ cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
     }
     h->launches += 4;
     double r[16] = {0};
+    unsigned mvbits = 0;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(r, h->dout, 16 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    if (h->sdiag && h->step > 0)
+        CK(cudaMemcpyAsync(&mvbits, h->sdiag + ((h->step - 1) & 1) * h->sdiag_stride, sizeof(unsigned),
+                           cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    if (!h->plain) {
+        float m2;
+        std::memcpy(&m2, &mvbits, sizeof(m2));
+        r[1] = std::max(r[1], (double)m2);
+    }
     out->mass = r[0];
     out->max_speed = std::sqrt(r[1]);
     out->nonfinite = r[2] != 0.0;
@@ -801,6 +836,7 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     cudaMemcpyAsync(sf0a, h->f0[P0], n * 4, cudaMemcpyDeviceToDevice, h->st);
     cudaMemcpyAsync(srho, h->rho, n * 4, cudaMemcpyDeviceToDevice, h->st);
     auto k = make_kparams<float>(h);
+    k.mvmax = nullptr;  // scratch launches leave the diagnostics alone
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -972,6 +1008,8 @@ cpmp_status batch_upload(cpmp_batch *b)
 void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
 {
     const int P = (int)(b->boxes[0]->step & 1);
+    const size_t nb = b->boxes.size();
+    cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
     fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params, b->d_boxes,
                      (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P, b->d_counter, b->st, hook);
     if (!bookkeeping) return;
@@ -1024,6 +1062,7 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
         if (b->d_params) cudaFree(b->d_params);
         if (b->d_boxes) cudaFree(b->d_boxes);
         if (b->d_counter) cudaFree(b->d_counter);
+        if (b->d_mvmax) cudaFree(b->d_mvmax);
         cudaStreamDestroy(b->st);
     };
     for (int i = 0; i < count; ++i) {
@@ -1047,9 +1086,18 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
     cpmp_status s;
     if ((s = dalloc((void **)&b->d_params, count * sizeof(KParams<float>), "batch params")) != CPMP_OK ||
         (s = dalloc((void **)&b->d_boxes, count * sizeof(BatchBox), "batch boxes")) != CPMP_OK ||
-        (s = dalloc((void **)&b->d_counter, sizeof(unsigned), "batch counter")) != CPMP_OK) {
+        (s = dalloc((void **)&b->d_counter, sizeof(unsigned), "batch counter")) != CPMP_OK ||
+        (s = dalloc((void **)&b->d_mvmax, 2 * count * sizeof(unsigned), "batch mv max")) != CPMP_OK) {
         cleanup();
         return s;
+    }
+    CK(cudaMemset(b->d_mvmax, 0, 2 * count * sizeof(unsigned)));
+    for (int i = 0; i < count; ++i) {  // the boxes' diagnostics live in the batch's array
+        cpmp_handle *h = b->boxes[i];
+        if (h->sdiag && h->sdiag_owned) cudaFree(h->sdiag);
+        h->sdiag = b->d_mvmax + i;
+        h->sdiag_stride = count;
+        h->sdiag_owned = false;
     }
     if ((s = batch_upload(b.get())) != CPMP_OK) {
         cleanup();
@@ -1205,6 +1253,8 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
     }
     const FusedTile keep = b->tile;
     const long long step_keep = b->boxes[0]->step;
+    std::vector<unsigned> mv_keep(2 * b->boxes.size());  // the scratch steps overwrite the diagnostics
+    cudaMemcpyAsync(mv_keep.data(), b->d_mvmax, mv_keep.size() * sizeof(unsigned), cudaMemcpyDeviceToHost, b->st);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1249,6 +1299,7 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
     cudaStreamSynchronize(b->st);
     free_scratch();
     if (err != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(err));
+    CK(cudaMemcpy(b->d_mvmax, mv_keep.data(), mv_keep.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
     b->tile = best;
     for (cpmp_handle *h : b->boxes) h->tile = best;
     if (b->gexec) {
@@ -1309,6 +1360,7 @@ void cpmp_batch_destroy(cpmp_batch *b)
     cudaFree(b->d_params);
     cudaFree(b->d_boxes);
     cudaFree(b->d_counter);
+    cudaFree(b->d_mvmax);
     cudaStreamDestroy(b->st);
     b->hook.reset();
     delete b;

@@ -336,6 +336,16 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Warp maximum of the threads' max |MV|^2, one atomicMax per warp (the bits
+// of a non-negative float order as unsigned integers).
+__device__ __forceinline__ void mvmax_flush(const KParams<float> &p, int P, float mv2)
+{
+    if (!p.mvmax) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mv2 = fmaxf(mv2, __shfl_xor_sync(0xffffffffu, mv2, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(p.mvmax + P * p.mvmax_stride, __float_as_uint(mv2));
+}
+
 // The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
 // addressing): as base pointers in the launch's parameter space, so that an
 // access is one multiply-add on a constant operand, or in shared memory (the
@@ -534,6 +544,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
 
     const int mc = (ty + 3) * MZ + (tz + 3);
     const int ac = (ty + 1) * AZ + (tz + 1);
+    float mv2 = 0.f;  // max |MV|^2 of this thread's nodes
     for (int x = x0; x < x1; ++x) {
         cp_async_wait_all();
         __syncthreads();  // rho(x+3+L), f0(x+1) landed; plane x-1 fully done
@@ -605,6 +616,11 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             const float ux = (f[1] + f[7] + f[9] + f[11] + f[13] - f[2] - f[8] - f[10] - f[12] - f[14]) * ir;
             const float uy = (f[3] + f[7] + f[8] + f[15] + f[17] - f[4] - f[9] - f[10] - f[16] - f[18]) * ir;
             const float uz = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) * ir;
+            {   // MV = u + F / (2 rho), the reference's MacroCalculate velocity
+                const float hr = 0.5f * ir;
+                const float vx = fmaf(Fx, hr, ux), vy = fmaf(Fy, hr, uy), vz = fmaf(Fz, hr, uz);
+                mv2 = fmaxf(mv2, fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
+            }
             if (p.qp) {
                 float qp[Q];
 #pragma unroll
@@ -657,6 +673,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
         for (int q = 0; q < Q - 1; ++q) hv[q] = hn[q];
     }
     cp_async_wait_all();
+    mvmax_flush(p, P, mv2);
 }
 
 // One box: CTA (bx, by, bz) owns z tile bx, y tile by and x chunk bz.

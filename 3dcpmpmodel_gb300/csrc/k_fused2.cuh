@@ -287,6 +287,7 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, cons
 
     const int mc = (ty + 3) * MZ + (tz + 3);
     const int ac = (ty + 1) * AZ + (tz + 2);  // even
+    float mv2 = 0.f;  // max |MV|^2 of this thread's fluid nodes
     for (int x = x0; x < x1; ++x) {
         cp_async_wait_all();
         __syncthreads();
@@ -336,6 +337,13 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, cons
             const float2 uz = mul(sub(sub(sub(sub(sub(add(add(add(add(f[5], f[11]), f[12]), f[15]), f[16]), f[6]),
                                                   f[13]), f[14]), f[17]), f[18]), ir);
             const float2 Fx = make_float2(FA[0], FB[0]), Fy = make_float2(FA[1], FB[1]), Fz = make_float2(FA[2], FB[2]);
+            {   // MV = u + F / (2 rho) on the pair's fluid nodes
+                const float2 hr = mul(K(0.5f), ir);
+                const float2 vx = fma(Fx, hr, ux), vy = fma(Fy, hr, uy), vz = fma(Fz, hr, uz);
+                const float2 v2 = fma(vx, vx, fma(vy, vy, mul(vz, vz)));
+                if (inA) mv2 = fmaxf(mv2, v2.x);
+                if (inB) mv2 = fmaxf(mv2, v2.y);
+            }
             if (p.qp) {
                 float qa[Q], qb[Q];
 #pragma unroll
@@ -426,6 +434,7 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, cons
         for (int q = 0; q < Q - 1; ++q) hv[q] = hn[q];
     }
     cp_async_wait_all();
+    mvmax_flush(p, P, mv2);
 }
 
 // Registers: at most 128 per thread for 4-byte storage pairs and the

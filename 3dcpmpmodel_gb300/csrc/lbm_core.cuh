@@ -55,6 +55,10 @@ struct KParams {
     R ts[Q];
     R omts[Q];         // 1 - ts, rounded once on the host
     const R *wall;     // [2][dx*dy] wall chemical potential, bottom then top
+    // FUSED collide: max over fluid nodes of |MV|^2 (float bits, atomicMax)
+    // into mvmax[P * mvmax_stride] at parity P (null: not accumulated)
+    unsigned *mvmax;
+    int mvmax_stride;
 };
 
 __host__ __device__ __forceinline__ bool solid_k(int wall_mode, int k, int dz)

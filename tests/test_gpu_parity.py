@@ -215,6 +215,26 @@ def test_paired_kernel_matches_single_node_kernel(cpmp, cfg, storage):
         assert np.array_equal(d, runs[0][1])
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_fused_max_speed_is_that_of_the_last_collision(cpmp, storage):
+    """The FUSED collide accumulates max |MV| (MV = u + F / 2 rho) of the
+    state it collides, as the reference's MV array is written by its collide
+    kernel; cpmp_reduce after a step reports it.  Checked against MV
+    recomputed from the state before that step (another evaluation order of
+    the same FP32 formulas)."""
+    s = solver_for(cpmp, WALLED, scheme="fused", storage=storage)
+    s.step(20)
+    mv = s.get("mv").reshape(3, -1)
+    fluid = s.get("type") == 1
+    want = float(np.sqrt((mv ** 2).sum(0)[fluid].max()))
+    s.step(1)
+    got = s.reduce()["max_speed"]
+    assert want > 0 and got == pytest.approx(want, rel=1e-4)
+    s.step(2)  # the graph-replayed steps accumulate it too
+    assert s.reduce()["max_speed"] > 0
+    s.close()
+
+
 def test_autotune_keeps_the_state(cpmp):
     s = solver_for(cpmp, WALLED, scheme="fused", storage="f16")
     s.step(3)
