@@ -275,7 +275,9 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        k_density<S><<<g, dim3(DENSITY_BZ, DENSITY_BY), 0, st>>>(p, P, (const S *)h, f0, rho);
+        SlotTable<const S> slots;
+        for (int k = 0; k < Q - 1; ++k) slots.q[k] = (const S *)h + (size_t)p.n * k;
+        k_density<S><<<g, dim3(DENSITY_BZ, DENSITY_BY), 0, st>>>(p, P, (const S *)h, slots, f0, rho);
     });
     hook_end(hook, K_DENSITY, st);
 }

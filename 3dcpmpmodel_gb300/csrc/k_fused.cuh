@@ -51,6 +51,28 @@ __device__ __forceinline__ __nv_bfloat16 f2s<__nv_bfloat16>(float v) { return __
 
 __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
+// The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
+// addressing): as base pointers in the launch's parameter space, so that an
+// access is one multiply-add on a constant operand, in shared memory (the
+// items of a batch, whose boxes differ), or as h + n k.
+template <class S>
+struct SlotTable {
+    S *q[Q - 1];
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
+};
+template <class S>
+struct SlotBase {
+    S *h;
+    unsigned n;
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return h + (size_t)n * (unsigned)k + idx; }
+};
+template <class S>
+struct SlotShared {
+    S *const *q;  // shared-memory copy of the item's box pointers
+    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
+};
+
+
 // w_q / w_0 and 1 / w_q
 __host__ __device__ __forceinline__ constexpr float ratio0(int q) { return q <= 6 ? 1.0f / 6.0f : 1.0f / 12.0f; }
 __host__ __device__ __forceinline__ constexpr float inv_w(int q) { return q <= 6 ? 18.0f : 36.0f; }
@@ -173,22 +195,21 @@ __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
 // index and N even, so it is that of cz(q)) and aligned pairs are vector
 // loads; otherwise all moving-population and anchor loads are scalar.  Every
 // load is issued before the first add so their latencies overlap.
-template <class S, int P, bool EVEN>
-__device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const S *__restrict__ h,
+template <class S, int P, bool EVEN, class SL>
+__device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const SL &slots,
                                                   const float *__restrict__ f0, float *__restrict__ rho,
                                                   unsigned I)
 {
     // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
-    const unsigned n = (unsigned)p.n;
     const int plane = p.dy * p.dz;
     float2 hv[Q - 1], a[Q - 1];
 #pragma unroll
     for (int q = 1; q < Q; ++q) {
         const int off = cx(q) * plane + cy(q) * p.dz + cz(q);
         const unsigned src = I - (unsigned)off;
-        const size_t hi = P == 0 ? (size_t)n * (unsigned)(q - 1) + I : (size_t)n * (unsigned)(opp(q) - 1) + src;
+        const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, src);
         const bool odd_off = (cz(q) & 1) != 0;
-        hv[q - 1] = load_pair<S>(h + hi, EVEN && (P == 0 || !odd_off));
+        hv[q - 1] = load_pair<S>(hp, EVEN && (P == 0 || !odd_off));
         a[q - 1] = load_pair<float>(f0 + src, EVEN && !odd_off);
     }
     float2 r = *reinterpret_cast<const float2 *>(f0 + I);
@@ -205,12 +226,11 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
 // (wall_mode 1): the paired path's sums (r += w_q h_q, then r += (w_q / w_0)
 // a_q, q in order, fused multiply-adds) with each source across the wall
 // layer (k = 3 or dz - 4) replaced by the node's own slot and rest population.
-template <class S>
-__device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P, const S *__restrict__ h,
+template <class S, class SL>
+__device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P, const SL &slots,
                                                   const float *__restrict__ f0, float *__restrict__ rho,
                                                   unsigned I, int k)
 {
-    const unsigned n = (unsigned)p.n;
     const int plane = p.dy * p.dz;
     const bool lo = k == 3, hi = k == p.dz - 4;
     const float a0 = f0[I];
@@ -219,8 +239,7 @@ __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P
     for (int q = 1; q < Q; ++q) {
         const unsigned src = I - (unsigned)(cx(q) * plane + cy(q) * p.dz + cz(q));
         const bool ss = (cz(q) == 1 && lo) || (cz(q) == -1 && hi);
-        const size_t hi_idx = (P == 0 || ss) ? (size_t)n * (unsigned)(q - 1) + I : (size_t)n * (unsigned)(opp(q) - 1) + src;
-        hv[q - 1] = s2f<S>(h[hi_idx]);
+        hv[q - 1] = s2f<S>(*((P == 0 || ss) ? slots(q - 1, I) : slots(opp(q) - 1, src)));
         a[q - 1] = ss ? a0 : f0[src];
     }
     float r = a0;
@@ -236,10 +255,10 @@ __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P
 // outside [0, dz)); the node index of k0 is even (see pair_k0).  Pairs next
 // to a z wall in an x/y-interior column take density_wall_node, pairs at a
 // periodic edge the general per-node path.
-template <class S>
+template <class S, class SL>
 __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, const S *__restrict__ h,
-                                             const float *__restrict__ f0, float *__restrict__ rho, int i, int j,
-                                             int k0)
+                                             const SL &slots, const float *__restrict__ f0,
+                                             float *__restrict__ rho, int i, int j, int k0)
 {
     const bool in0 = k0 >= 0 && k0 < p.dz, in1 = k0 + 1 >= 0 && k0 + 1 < p.dz;
     const bool xy = i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy;
@@ -247,8 +266,8 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
     if (!fast) {
         const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
         if (xy && p.wall_mode == 1) {
-            if (in0 && !solid_k(1, k0, p.dz)) density_wall_node<S>(p, P, h, f0, rho, I, k0);
-            if (in1 && !solid_k(1, k0 + 1, p.dz)) density_wall_node<S>(p, P, h, f0, rho, I + 1, k0 + 1);
+            if (in0 && !solid_k(1, k0, p.dz)) density_wall_node<S>(p, P, slots, f0, rho, I, k0);
+            if (in1 && !solid_k(1, k0 + 1, p.dz)) density_wall_node<S>(p, P, slots, f0, rho, I + 1, k0 + 1);
             return;
         }
         if (in0) density_node<S>(p, P, h, f0, rho, i, j, k0);
@@ -257,11 +276,11 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
     }
     const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
     if ((p.dz & 1) == 0) {
-        if (P == 0) density_pair_fast<S, 0, true>(p, h, f0, rho, I);
-        else density_pair_fast<S, 1, true>(p, h, f0, rho, I);
+        if (P == 0) density_pair_fast<S, 0, true>(p, slots, f0, rho, I);
+        else density_pair_fast<S, 1, true>(p, slots, f0, rho, I);
     } else {
-        if (P == 0) density_pair_fast<S, 0, false>(p, h, f0, rho, I);
-        else density_pair_fast<S, 1, false>(p, h, f0, rho, I);
+        if (P == 0) density_pair_fast<S, 0, false>(p, slots, f0, rho, I);
+        else density_pair_fast<S, 1, false>(p, slots, f0, rho, I);
     }
 }
 
@@ -283,13 +302,19 @@ constexpr int DENSITY_BZ = 32, DENSITY_BY = 4;
 template <class S>
 __global__ void __launch_bounds__(DENSITY_BZ *DENSITY_BY) k_density(KParams<float> p, int P,
                                                                      const S *__restrict__ h,
+                                                                     SlotTable<const S> slots,
                                                                      const float *__restrict__ f0,
                                                                      float *__restrict__ rho)
 {
+    const int ppc = pairs_per_column(p.dz);
     const int t = blockIdx.x * DENSITY_BZ + threadIdx.x, j = blockIdx.y * DENSITY_BY + threadIdx.y;
-    if (t >= pairs_per_column(p.dz) || j >= p.dy) return;
+    if (t >= ppc || j >= p.dy) return;
     const int i = blockIdx.z;
-    density_pair<S>(p, P, h, f0, rho, i, j, pair_k0(p, i, j, t));
+    // pairs rotated by two: the two wall-adjacent pairs of a walled column
+    // (1 and ppc - 2) land in the column's last warp, the only one whose
+    // lanes then take two paths
+    const int tr = (t + 2) % ppc;
+    density_pair<S>(p, P, h, slots, f0, rho, i, j, pair_k0(p, i, j, tr));
 }
 
 // --------------------------------------------------------- fused step ----
@@ -345,21 +370,6 @@ __device__ __forceinline__ void mvmax_flush(const KParams<float> &p, int P, floa
     for (int o = 16; o > 0; o >>= 1) mv2 = fmaxf(mv2, __shfl_xor_sync(0xffffffffu, mv2, o));
     if ((threadIdx.x & 31) == 0) atomicMax(p.mvmax + P * p.mvmax_stride, __float_as_uint(mv2));
 }
-
-// The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
-// addressing): as base pointers in the launch's parameter space, so that an
-// access is one multiply-add on a constant operand, or in shared memory (the
-// items of a batch, whose boxes differ).
-template <class S>
-struct SlotTable {
-    S *q[Q - 1];
-    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
-};
-template <class S>
-struct SlotShared {
-    S *const *q;  // shared-memory copy of the item's box pointers
-    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
-};
 
 // One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
 // x.  Shared-memory rings:
@@ -744,7 +754,8 @@ __global__ void __launch_bounds__(128) k_density_batch(const KParams<float> *__r
     if (e >= p.dy * per_col) return;
     const BatchBox &bx = boxes[b];
     const int j = e / per_col, t = e - j * per_col;
-    density_pair<S>(p, P, (const S *)bx.h, bx.f0[P], bx.rho[P], i, j, pair_k0(p, i, j, t));
+    density_pair<S>(p, P, (const S *)bx.h, SlotBase<const S>{(const S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.rho[P], i,
+                    j, pair_k0(p, i, j, t));
 }
 
 template <class S, int TY, int TZ, int L>

@@ -114,7 +114,9 @@ typedef struct cpmp_droplet {
  * (FluidCuda.cu:1159-1199). */
 typedef struct cpmp_diag {
     double mass;          /* FP64 sum of rho over fluid nodes */
-    double max_speed;     /* max |MV| over fluid nodes */
+    double max_speed;     /* max |MV| over fluid nodes, MV = u + F / (2 rho) of the
+                             state the last step collided (the reference's MV array,
+                             written by its collide kernel; 0 before the first step) */
     int nonfinite;        /* 1 if any fluid density is NaN or negative */
     double ca_left, ca_right, ca_cap; /* contact angles (degrees), slice j = DY/2 */
     double x_left, x_right;           /* contact-line positions */
@@ -167,7 +169,9 @@ cpmp_status cpmp_sync(cpmp_handle *h);
 cpmp_status cpmp_get_field(cpmp_handle *h, cpmp_field f, int dtype, void *host_dst, size_t bytes);
 
 /* Host-to-device copy of RHO, U or DIST (seeded states for parity runs).
- * Setting DIST also recomputes RHO and U from it on fluid nodes. */
+ * Setting DIST also recomputes RHO and U from it on fluid nodes; on the
+ * FUSED scheme a page-locked host_src is read by the encode kernels in place
+ * (no device staging copy). */
 cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *host_src,
                            size_t bytes);
 
