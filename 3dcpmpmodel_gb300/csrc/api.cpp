@@ -156,9 +156,8 @@ cpmp_status dalloc(void **ptr, size_t bytes, const char *what)
 FusedTile default_tile(const cpmp_params &p)
 {
     int ty = 8, tz = 32;
-    if (p.dy <= 2) { ty = 1; tz = 128; }
-    else if (p.dy < 8) { ty = 4; tz = 32; }
-    if (p.dz <= 32 && p.dy >= 8) { ty = 8; tz = 32; }
+    if (p.dy < 8) { ty = 4; tz = 32; }
+    if (p.dz <= 16) { ty = p.dy < 16 ? 8 : 16; tz = 16; }
     const long long tiles = (long long)((p.dz + tz - 1) / tz) * ((p.dy + ty - 1) / ty);
     // aim for >= 4 CTAs per SM on a 152-SM part, but march at least 8 planes
     long long xl = (long long)p.dx * tiles / (4 * 152);

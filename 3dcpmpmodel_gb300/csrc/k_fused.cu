@@ -111,7 +111,7 @@ __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, con
 // ------------------------------------------------------------- dispatch ----
 namespace {
 // (ty, tz, nodes per thread)
-constexpr int kTiles[][3] = {{4, 32, 1}, {8, 32, 1}, {16, 32, 1}, {2, 64, 1}, {1, 128, 1},
+constexpr int kTiles[][3] = {{4, 32, 1}, {8, 32, 1}, {16, 32, 1}, {16, 16, 1}, {8, 16, 1},
                              {8, 32, 2}, {16, 32, 2}, {8, 64, 2}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
@@ -144,8 +144,8 @@ void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, 
     if (t.ty == 4 && t.tz == 32) launch_collide_t<S, 4, 32, L>(p, P, t, h, f0c, f0n, rho, st);
     else if (t.ty == 8 && t.tz == 32) launch_collide_t<S, 8, 32, L>(p, P, t, h, f0c, f0n, rho, st);
     else if (t.ty == 16 && t.tz == 32) launch_collide_t<S, 16, 32, L>(p, P, t, h, f0c, f0n, rho, st);
-    else if (t.ty == 2 && t.tz == 64) launch_collide_t<S, 2, 64, L>(p, P, t, h, f0c, f0n, rho, st);
-    else launch_collide_t<S, 1, 128, L>(p, P, t, h, f0c, f0n, rho, st);
+    else if (t.ty == 16 && t.tz == 16) launch_collide_t<S, 16, 16, L>(p, P, t, h, f0c, f0n, rho, st);
+    else launch_collide_t<S, 8, 16, L>(p, P, t, h, f0c, f0n, rho, st);
 }
 
 bool fused2_set_attr(int storage, int lap_order, int ty, int tz, int max_smem)
@@ -185,8 +185,8 @@ void set_attr_l(int si, int max_smem)
     set_attr_t<S, 4, 32, L>(si, max_smem);
     set_attr_t<S, 8, 32, L>(si, max_smem);
     set_attr_t<S, 16, 32, L>(si, max_smem);
-    set_attr_t<S, 2, 64, L>(si, max_smem);
-    set_attr_t<S, 1, 128, L>(si, max_smem);
+    set_attr_t<S, 16, 16, L>(si, max_smem);
+    set_attr_t<S, 8, 16, L>(si, max_smem);
 }
 }  // namespace
 
@@ -306,8 +306,8 @@ void batch_collide_l(const FusedTile &t, const KParams<float> *params, const Bat
     if (t.ty == 4 && t.tz == 32) batch_collide_t<S, 4, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
     else if (t.ty == 8 && t.tz == 32) batch_collide_t<S, 8, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
     else if (t.ty == 16 && t.tz == 32) batch_collide_t<S, 16, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else if (t.ty == 2 && t.tz == 64) batch_collide_t<S, 2, 64, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else batch_collide_t<S, 1, 128, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else if (t.ty == 16 && t.tz == 16) batch_collide_t<S, 16, 16, L>(params, boxes, nbox, total, P, t.xl, counter, st);
+    else batch_collide_t<S, 8, 16, L>(params, boxes, nbox, total, P, t.xl, counter, st);
 }
 }  // namespace
 

@@ -178,7 +178,7 @@ def test_fused_result_is_independent_of_tile(cpmp, storage):
     the same decode and summation order, so any tile gives the same bits."""
     cfg = dict(dx=48, dy=24, dz=40, radius=9.0, width=4.0, base_pt=-0.04)
     runs = []
-    for ty, tz, xl, npt in ((8, 32, 16, 1), (4, 32, 7, 1), (1, 128, 48, 1), (2, 64, 5, 1), (8, 32, 16, 2),
+    for ty, tz, xl, npt in ((8, 32, 16, 1), (4, 32, 7, 1), (16, 16, 48, 1), (8, 16, 5, 1), (8, 32, 16, 2),
                             (16, 32, 7, 2), (8, 64, 48, 2)):
         s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
         s.set_tile(ty, tz, xl, npt)
