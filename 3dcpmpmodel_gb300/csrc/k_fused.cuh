@@ -200,17 +200,20 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
                                                   const float *__restrict__ f0, float *__restrict__ rho,
                                                   unsigned I)
 {
-    // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
+    // node indices are 32-bit (the FUSED scheme keeps N below 2^32); the
+    // neighbour offsets are applied as signed pointer offsets from the node's
+    // own addresses, so the nine in-plane parts are shared and the z part is
+    // an immediate
     const int plane = p.dy * p.dz;
+    const float *fI = f0 + I;
     float2 hv[Q - 1], a[Q - 1];
 #pragma unroll
     for (int q = 1; q < Q; ++q) {
         const int off = cx(q) * plane + cy(q) * p.dz + cz(q);
-        const unsigned src = I - (unsigned)off;
-        const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, src);
+        const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, I) - off;
         const bool odd_off = (cz(q) & 1) != 0;
         hv[q - 1] = load_pair<S>(hp, EVEN && (P == 0 || !odd_off));
-        a[q - 1] = load_pair<float>(f0 + src, EVEN && !odd_off);
+        a[q - 1] = load_pair<float>(fI - off, EVEN && !odd_off);
     }
     float2 r = *reinterpret_cast<const float2 *>(f0 + I);
 #pragma unroll
@@ -517,6 +520,16 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
                 hv[q - 1] = *(ss ? slot(q - 1, I)
                                  : slot(opp(q) - 1, I - (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))));
             }
+        } else if (p.wall_mode == 1) {
+            // walls at a periodic x or y edge: x and y wrap, z does not
+            const bool lo = gz == 3, hi = gz == p.dz - 4;
+#pragma unroll
+            for (int q = 1; q < Q; ++q) {
+                const bool ss = (cz(q) == 1 && lo) || (cz(q) == -1 && hi);
+                const int si = wrap1(gx - cx(q), p.dx), sj = wrap1(gy - cy(q), p.dy);
+                hv[q - 1] = *(ss ? slot(q - 1, I)
+                                 : slot(opp(q) - 1, (unsigned)si * plane + (unsigned)(sj * p.dz + gz - cz(q))));
+            }
         } else {
 #pragma unroll
             for (int q = 1; q < Q; ++q) {
@@ -665,6 +678,15 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
                 for (int q = 1; q < Q; ++q) {
                     const bool ss = (cz(q) == -1 && lo) || (cz(q) == 1 && hi);
                     *(ss ? slot(opp(q) - 1, I) : slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)))) =
+                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                }
+            } else if (p.wall_mode == 1) {
+                const bool lo = gz == 3, hi = gz == p.dz - 4;
+#pragma unroll
+                for (int q = 1; q < Q; ++q) {
+                    const bool ss = (cz(q) == -1 && lo) || (cz(q) == 1 && hi);
+                    const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy);
+                    *(ss ? slot(opp(q) - 1, I) : slot(q - 1, (unsigned)di * plane + (unsigned)(dj * p.dz + gz + cz(q)))) =
                         f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
                 }
             } else {
