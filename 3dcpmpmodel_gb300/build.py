@@ -2,7 +2,7 @@
 
 Every translation unit is compiled with nvcc for sm_103a only, in parallel,
 into ``_build/``; the shared library links the CUDA runtime statically so it
-depends on nothing but the driver.
+depends on nothing but the CUDA driver library.
 """
 from __future__ import annotations
 

@@ -1145,6 +1145,8 @@ cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
             // the second step of the pair runs at odd parity on the same tables
             {
                 const int P = 1;
+                const size_t nb = b->boxes.size();
+                cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
                 fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params,
                                  b->d_boxes, (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P,
                                  b->d_counter, b->st, nullptr);

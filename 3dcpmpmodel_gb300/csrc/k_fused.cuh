@@ -328,34 +328,6 @@ __device__ __forceinline__ int wrap_small(int a, int n)
     return a;
 }
 
-template <int TY, int TZ, int L>
-struct FusedGeom {
-    static constexpr int RH = 3 + L;                 // rho halo (y, z)
-    static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
-    // ring sizes are powers of two so a plane's slot is (x & (size - 1)),
-    // also for the negative x of the prologue
-    static constexpr int NR = 8;                     // rho planes x+3-L .. x+4+L (one prefetched)
-    static_assert(2 * L + 2 <= NR, "rho ring too small");
-    static constexpr int MY = TY + 6, MZ = TZ + 6;   // (rho, mu) pairs, halo 3, planes x-3..x+3
-    static constexpr int AY = TY + 2, AZ = TZ + 2;   // rest populations, halo 1, planes x-1..x+2
-    static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
-    static constexpr int RM_PAIRS = 8 * MY * MZ;     // (rho, mu) planes x-3 .. x+3 (+1 being written)
-    static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
-    // per-tile element tables: (centre in the rho plane | solid flag, wall
-    // offset) of each (rho, mu) element; plane offsets of the rho and anchor
-    // ring elements; wrapped y, z rows
-    static constexpr int MTAB_INT2 = MY * MZ;
-    static constexpr int TAB_INTS = 2 * RY + RZ + RY * RZ + AY * AZ;
-    static constexpr size_t BASE_BYTES = sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
-                                         sizeof(float) * F0_FLOATS + sizeof(int2) * MTAB_INT2 +
-                                         sizeof(int) * TAB_INTS;
-    template <class S>
-    static constexpr size_t bytes()
-    {
-        return ((BASE_BYTES + 15) / 16) * 16;
-    }
-};
-
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -364,86 +336,93 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Warp maximum of the threads' max |MV|^2, one atomicMax per warp (the bits
-// of a non-negative float order as unsigned integers).
-__device__ __forceinline__ void mvmax_flush(const KParams<float> &p, int P, float mv2)
-{
-    if (!p.mvmax) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mv2 = fmaxf(mv2, __shfl_xor_sync(0xffffffffu, mv2, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(p.mvmax + P * p.mvmax_stride, __float_as_uint(mv2));
-}
-
-// One CTA owns a TY x TZ column tile of (y, z) and marches over xl planes of
-// x.  Shared-memory rings:
+// The shared-memory rings of a fused-collide CTA that owns a TY x TZ column
+// tile of (y, z) and marches over x with NT threads:
 //   rho : planes x+3-L .. x+4+L, halo 3+L (L = 2: five-point Laplacian, 3: seven-point)
 //   (rho, mu) pairs: planes x-3 .. x+3, halo 3 (the force stencil's support)
-//   f0  : planes x-1 .. x+2, halo 1 (anchors of the moving populations)
-// The next plane's rho and f0 are copied in with cp.async while the current
-// plane is computed, and the next plane's moving populations are loaded into
-// registers, so global-memory latency overlaps the stencil and collision work.
-// For output plane x: mu(x+3) is evaluated (EOS + Laplacian; wall potential on
-// solid nodes), then every fluid node of plane x computes
-// F = -rho grad7(mu) + grad7(rho)/3, decodes its populations, collides (MRT +
-// exact-difference forcing) and streams A-A in place.
-template <class S, int TY, int TZ, int L, class SL>
-__device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const SL &slots,
-                                           const float *__restrict__ f0c, float *__restrict__ f0n,
-                                           const float *__restrict__ rho, const int z0, const int y0,
-                                           const int x0, const int xl, float4 *smem4)
-{
-    using G = FusedGeom<TY, TZ, L>;
-    constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
-    constexpr int AY = G::AY, AZ = G::AZ;
-    constexpr int NT = TY * TZ;
-    float *srho = reinterpret_cast<float *>(smem4);
-    float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
-    float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
-    int2 *mtab = reinterpret_cast<int2 *>(sf0 + G::F0_FLOATS);
-    int *tabY = reinterpret_cast<int *>(mtab + G::MTAB_INT2);
-    int *tabZ = tabY + RY;
-    int *tabYdz = tabZ + RZ;  // wrapped y row times dz
-    int *offR = tabYdz + RY;  // rho ring element -> offset in its x plane
-    int *offA = offR + RY * RZ;  // anchor ring element -> offset in its x plane
+//   f0  : planes x-1 .. x+2, halo 1 in y and AZH in z (anchors of the moving
+//         populations; AZH = 2 keeps node pairs on even indices)
+// Ring sizes are powers of two so a plane's slot is (x & (size - 1)), also for
+// the negative x of the prologue.  Per-tile element tables (built once,
+// fixed for the whole march) give each ring element its offset in an x plane
+// and each (rho, mu) element its centre in the rho plane, solid flag and wall
+// offset, so the per-plane loops run a fixed trip count without division.
+template <int TY, int TZ, int L, int NT, int AZH>
+struct FusedRings {
+    static constexpr int RH = 3 + L;
+    static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
+    static constexpr int NR = 8;
+    static_assert(2 * L + 2 <= NR, "rho ring too small");
+    static constexpr int MY = TY + 6, MZ = TZ + 6;
+    static constexpr int AY = TY + 2, AZ = TZ + 2 * AZH;
+    static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
+    static constexpr int RM_PAIRS = 8 * MY * MZ;
+    static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
+    static constexpr int MTAB_INT2 = MY * MZ;
+    static constexpr int TAB_INTS = 2 * RY + RZ + RY * RZ + AY * AZ;
+    static constexpr size_t BYTES = ((sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
+                                      sizeof(float) * F0_FLOATS + sizeof(int2) * MTAB_INT2 +
+                                      sizeof(int) * TAB_INTS + 15) / 16) * 16;
+    static constexpr int KR = (RY * RZ + NT - 1) / NT, KA = (AY * AZ + NT - 1) / NT;
+    static constexpr int KM = (MY * MZ + NT - 1) / NT;
 
-    const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
-    const int x1 = min(x0 + xl, p.dx);
-    // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
-    const unsigned plane = (unsigned)(p.dy * p.dz);
-    auto slot = [&](int q, unsigned idx) -> S * { return slots(q, idx); };
-    const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
-    const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
+    const KParams<float> &p;
+    const float *rho, *f0c;
+    unsigned plane;
+    EosFast eos;
+    float *srho;
+    float2 *srm;
+    float *sf0;
+    int2 *mtab;
+    int *tabY, *tabZ, *tabYdz, *offR, *offA;
 
-    // wrapped y / z coordinates of the halo rows and columns, then the
-    // element tables the per-plane loops read (fixed for the whole march)
-    for (int e = threadIdx.x; e < RY + RZ; e += NT) {
-        if (e < RY) {
-            tabY[e] = wrap_small(y0 - RH + e, p.dy);
-            tabYdz[e] = tabY[e] * p.dz;
-        } else {
-            tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+    __device__ __forceinline__ FusedRings(const KParams<float> &p_, const float *rho_, const float *f0c_,
+                                          float4 *smem4)
+        : p(p_), rho(rho_), f0c(f0c_), plane((unsigned)(p_.dy * p_.dz)),
+          eos(make_eos_fast(p_.eos, p_.A, p_.B, p_.T))
+    {
+        srho = reinterpret_cast<float *>(smem4);
+        srm = reinterpret_cast<float2 *>(srho + RHO_FLOATS);
+        sf0 = reinterpret_cast<float *>(srm + RM_PAIRS);
+        mtab = reinterpret_cast<int2 *>(sf0 + F0_FLOATS);
+        tabY = reinterpret_cast<int *>(mtab + MTAB_INT2);
+        tabZ = tabY + RY;
+        tabYdz = tabZ + RZ;    // wrapped y row times dz
+        offR = tabYdz + RY;    // rho ring element -> offset in its x plane
+        offA = offR + RY * RZ; // anchor ring element -> offset in its x plane
+    }
+
+    // wrapped y / z coordinates of the halo rows and columns, then the element tables
+    __device__ __forceinline__ void setup(int y0, int z0)
+    {
+        for (int e = threadIdx.x; e < RY + RZ; e += NT) {
+            if (e < RY) {
+                tabY[e] = wrap_small(y0 - RH + e, p.dy);
+                tabYdz[e] = tabY[e] * p.dz;
+            } else {
+                tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
+            }
         }
+        __syncthreads();
+        for (int e = threadIdx.x; e < RY * RZ; e += NT) {
+            const int ly = e / RZ, lz = e - ly * RZ;
+            offR[e] = tabYdz[ly] + tabZ[lz];
+        }
+        for (int e = threadIdx.x; e < AY * AZ; e += NT) {
+            const int ly = e / AZ, lz = e - ly * AZ;
+            offA[e] = tabYdz[ly + RH - 1] + tabZ[lz + RH - AZH];
+        }
+        for (int e = threadIdx.x; e < MY * MZ; e += NT) {
+            const int my = e / MZ, mz = e - my * MZ;
+            const int c = (my + L) * RZ + (mz + L), gz = tabZ[mz + L];
+            const int woff = (gz < 3 ? 0 : p.dx * p.dy) + tabY[my + L];
+            mtab[e] = make_int2(solid_k(p.wall_mode, gz, p.dz) ? (int)((unsigned)c | 0x80000000u) : c, woff);
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < RY * RZ; e += NT) {
-        const int ly = e / RZ, lz = e - ly * RZ;
-        offR[e] = tabYdz[ly] + tabZ[lz];
-    }
-    for (int e = threadIdx.x; e < AY * AZ; e += NT) {
-        const int ly = e / AZ, lz = e - ly * AZ;
-        offA[e] = tabYdz[ly + RH - 1] + tabZ[lz + RH - 1];
-    }
-    for (int e = threadIdx.x; e < MY * MZ; e += NT) {
-        const int my = e / MZ, mz = e - my * MZ;
-        const int c = (my + L) * RZ + (mz + L), gz = tabZ[mz + L];
-        const int woff = (gz < 3 ? 0 : p.dx * p.dy) + tabY[my + L];
-        mtab[e] = make_int2(solid_k(p.wall_mode, gz, p.dz) ? (int)((unsigned)c | 0x80000000u) : c, woff);
-    }
-    __syncthreads();
 
-    // per-plane element loops: a fixed trip count, the last pass predicated
-    constexpr int KR = (RY * RZ + NT - 1) / NT, KA = (AY * AZ + NT - 1) / NT, KM = (MY * MZ + NT - 1) / NT;
-    auto issue_rho = [&](int xlog) {
+    __device__ __forceinline__ void issue_rho(int xlog)
+    {
         const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = srho + (xlog & (NR - 1)) * (RY * RZ);
 #pragma unroll
@@ -451,8 +430,9 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             const int e = threadIdx.x + k * NT;
             if ((k + 1) * NT <= RY * RZ || e < RY * RZ) cp_async4(dst + e, src + (unsigned)offR[e]);
         }
-    };
-    auto issue_f0 = [&](int xlog) {
+    }
+    __device__ __forceinline__ void issue_f0(int xlog)
+    {
         const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
         float *dst = sf0 + (xlog & 3) * (AY * AZ);
 #pragma unroll
@@ -460,8 +440,10 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             const int e = threadIdx.x + k * NT;
             if ((k + 1) * NT <= AY * AZ || e < AY * AZ) cp_async4(dst + e, src + (unsigned)offA[e]);
         }
-    };
-    auto comp_mu = [&](int xlog) {
+    }
+    // mu of plane xlog: EOS + Laplacian on fluid nodes, the wall potential on solid ones
+    __device__ __forceinline__ void comp_mu(int xlog)
+    {
         const int gx = wrap_small(xlog, p.dx);
         float2 *dst = srm + (xlog & 7) * (MY * MZ);
         auto rpl = [&](int xx) -> const float * { return srho + (xx & (NR - 1)) * (RY * RZ); };
@@ -494,7 +476,84 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             }
             dst[e] = make_float2(r0, fmaf(p.kk, mu0_fast(eos, r0), -p.ka * lap));
         }
-    };
+    }
+    // mu(x0-3 .. x0+2) evaluated; f0(x0-1 .. x0+1) and rho(x0+3+L) in flight
+    __device__ __forceinline__ void prologue(int x0)
+    {
+        for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) issue_rho(x);
+        issue_f0(x0 - 1);
+        issue_f0(x0);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        comp_mu(x0 - 3);
+        for (int x = x0 - 2; x <= x0 + 2; ++x) {
+            __syncthreads();
+            issue_rho(x + L);
+            cp_async_commit();
+            cp_async_wait_all();
+            __syncthreads();
+            comp_mu(x);
+        }
+        __syncthreads();
+        issue_rho(x0 + 3 + L);
+        issue_f0(x0 + 1);
+        cp_async_commit();
+    }
+    // start of output plane x: rho(x+3+L) and f0(x+1) landed, plane x-1 done
+    // by every thread; the next planes' copies go out (unless x is the last)
+    __device__ __forceinline__ void begin_plane(int x, bool more)
+    {
+        cp_async_wait_all();
+        __syncthreads();
+        if (more) {
+            issue_rho(x + 4 + L);
+            issue_f0(x + 2);
+        }
+        cp_async_commit();
+    }
+    __device__ __forceinline__ const float2 *rm_plane(int x) const { return srm + (x & 7) * (MY * MZ); }
+    __device__ __forceinline__ const float *f0_plane(int x) const { return sf0 + (x & 3) * (AY * AZ); }
+};
+
+// Warp maximum of the threads' max |MV|^2, one atomicMax per warp (the bits
+// of a non-negative float order as unsigned integers).
+__device__ __forceinline__ void mvmax_flush(const KParams<float> &p, int P, float mv2)
+{
+    if (!p.mvmax) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mv2 = fmaxf(mv2, __shfl_xor_sync(0xffffffffu, mv2, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(p.mvmax + P * p.mvmax_stride, __float_as_uint(mv2));
+}
+
+// One CTA owns a TY x TZ column tile of (y, z) (one node per thread) and
+// marches over xl planes of x with the rings of FusedRings.  The next plane's
+// rho and f0 are copied in with cp.async while the current plane is computed,
+// and the next plane's moving populations are loaded into registers, so
+// global-memory latency overlaps the stencil and collision work.  For output
+// plane x: mu(x+3) is evaluated (EOS + Laplacian; wall potential on solid
+// nodes), then every fluid node of plane x computes
+// F = -rho grad7(mu) + grad7(rho)/3, decodes its populations, collides (MRT +
+// exact-difference forcing) and streams A-A in place.
+template <int TY, int TZ, int L>
+using Rings1 = FusedRings<TY, TZ, L, TY * TZ, 1>;
+
+template <class S, int TY, int TZ, int L, class SL>
+__device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const SL &slots,
+                                           const float *__restrict__ f0c, float *__restrict__ f0n,
+                                           const float *__restrict__ rho, const int z0, const int y0,
+                                           const int x0, const int xl, float4 *smem4)
+{
+    using RG = Rings1<TY, TZ, L>;
+    constexpr int MZ = RG::MZ, AZ = RG::AZ;
+    const int tz = threadIdx.x % TZ, ty = threadIdx.x / TZ;
+    const int x1 = min(x0 + xl, p.dx);
+    // node indices are 32-bit (the FUSED scheme keeps N below 2^32)
+    const unsigned plane = (unsigned)(p.dy * p.dz);
+    auto slot = [&](int q, unsigned idx) -> S * { return slots(q, idx); };
+    const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
+    RG R(p, rho, f0c, smem4);
+    R.setup(y0, z0);
 
     const int gy = y0 + ty, gz = z0 + tz;
     const bool active = gy < p.dy && gz < p.dz && !solid_k(p.wall_mode, gz, p.dz);
@@ -542,50 +601,24 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
         }
     };
 
-    // prologue: mu(x0-3 .. x0+2); f0(x0-1 .. x0+1) and rho(x0+3+L) in flight
     S hv[Q - 1];
-    for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) issue_rho(x);
-    issue_f0(x0 - 1);
-    issue_f0(x0);
-    cp_async_commit();
-    cp_async_wait_all();
-    __syncthreads();
-    comp_mu(x0 - 3);
-    for (int x = x0 - 2; x <= x0 + 2; ++x) {
-        __syncthreads();
-        issue_rho(x + L);
-        cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
-        comp_mu(x);
-    }
-    __syncthreads();
-    issue_rho(x0 + 3 + L);
-    issue_f0(x0 + 1);
-    cp_async_commit();
+    R.prologue(x0);
     fetch(x0, hv);
 
     const int mc = (ty + 3) * MZ + (tz + 3);
     const int ac = (ty + 1) * AZ + (tz + 1);
     float mv2 = 0.f;  // max |MV|^2 of this thread's nodes
     for (int x = x0; x < x1; ++x) {
-        cp_async_wait_all();
-        __syncthreads();  // rho(x+3+L), f0(x+1) landed; plane x-1 fully done
-        if (x + 1 < x1) {
-            issue_rho(x + 4 + L);
-            issue_f0(x + 2);
-        }
-        cp_async_commit();
+        R.begin_plane(x, x + 1 < x1);
         S hn[Q - 1];
         if (x + 1 < x1) fetch(x + 1, hn);
-        comp_mu(x + 3);
+        R.comp_mu(x + 3);
         __syncthreads();
         if (active) {
             // force from the (rho, mu) ring
-
             const float2 *pl[7];
 #pragma unroll
-            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + ((x + d) & 7) * (MY * MZ);
+            for (int d = -3; d <= 3; ++d) pl[d + 3] = R.rm_plane(x + d);
             // (rho, mu) pairs: each first difference is one paired add and one
             // paired fma per stencil distance (Blackwell FADD2 / FFMA2)
             float2 g0 = make_float2(0.f, 0.f), g1 = g0, g2 = g0;  // (grad rho, grad mu) per axis
@@ -621,10 +654,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
 
             // decode with the sources' rest populations as anchors
 
-            const float *fa[3];
-            fa[0] = sf0 + ((x - 1) & 3) * (AY * AZ);  // plane x-1
-            fa[1] = sf0 + (x & 3) * (AY * AZ);        // plane x
-            fa[2] = sf0 + ((x + 1) & 3) * (AY * AZ);  // plane x+1
+            const float *fa[3] = {R.f0_plane(x - 1), R.f0_plane(x), R.f0_plane(x + 1)};
             const float a0 = fa[1][ac];
             float f[Q];
             f[0] = a0;
@@ -783,7 +813,7 @@ __global__ void __launch_bounds__(128) k_density_batch(const KParams<float> *__r
 template <class S, int TY, int TZ, int L>
 constexpr size_t fused_smem_bytes()
 {
-    return FusedGeom<TY, TZ, L>::template bytes<S>();
+    return Rings1<TY, TZ, L>::BYTES;
 }
 
 // ------------------------------------------------------------ init etc ----

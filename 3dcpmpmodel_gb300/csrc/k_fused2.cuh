@@ -51,26 +51,11 @@ struct SPair<float> {
     static __device__ __forceinline__ float zero() { return 0.f; }
 };
 
-// Shared-memory geometry of a TY x TZ node tile (TZ even, TY * TZ / 2
-// threads).  As FusedGeom, except that the rest-population ring has a z halo
-// of 2 so that every node pair sits on an even (8-byte aligned) index.
+// The rings of a TY x TZ node tile (TZ even, TY * TZ / 2 threads): those of
+// the one-node kernel, except that the rest-population ring has a z halo of 2
+// so that every node pair sits on an even (8-byte aligned) index.
 template <int TY, int TZ, int L>
-struct FusedGeom2 {
-    static_assert(TZ % 2 == 0, "node pairs need an even tile height");
-    static constexpr int RH = 3 + L;
-    static constexpr int RY = TY + 2 * RH, RZ = TZ + 2 * RH;
-    static constexpr int NR = 8;
-    static_assert(2 * L + 2 <= NR, "rho ring too small");
-    static constexpr int MY = TY + 6, MZ = TZ + 6;
-    static constexpr int AY = TY + 2, AZ = TZ + 4;
-    static constexpr int RHO_FLOATS = ((NR * RY * RZ + 3) / 4) * 4;
-    static constexpr int RM_PAIRS = 8 * MY * MZ;
-    static constexpr int F0_FLOATS = ((4 * AY * AZ + 3) / 4) * 4;
-    static constexpr int TAB_INTS = 2 * RY + RZ;
-    static constexpr size_t BYTES = ((sizeof(float) * RHO_FLOATS + sizeof(float2) * RM_PAIRS +
-                                      sizeof(float) * F0_FLOATS + sizeof(int) * TAB_INTS + 15) / 16) * 16;
-    static constexpr int THREADS = TY * TZ / 2;
-};
+using Rings2 = FusedRings<TY, TZ, L, TY * TZ / 2, 2>;
 
 // One CTA owns a TY x TZ column tile and marches over xl planes of x; see
 // fused_tile for the rings and the order of work per plane.
@@ -80,85 +65,19 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, cons
                                             const float *__restrict__ rho, const int z0, const int y0,
                                             const int x0, const int xl, float4 *smem4)
 {
-    using G = FusedGeom2<TY, TZ, L>;
+    static_assert(TZ % 2 == 0, "node pairs need an even tile height");
+    using RG = Rings2<TY, TZ, L>;
     using SP = SPair<S>;
     using T = typename SP::T;
     using namespace p2;
-    constexpr int RH = G::RH, RY = G::RY, RZ = G::RZ, NR = G::NR, MY = G::MY, MZ = G::MZ;
-    constexpr int AY = G::AY, AZ = G::AZ;
-    constexpr int NT = G::THREADS, TH = TZ / 2;
-    float *srho = reinterpret_cast<float *>(smem4);
-    float2 *srm = reinterpret_cast<float2 *>(srho + G::RHO_FLOATS);
-    float *sf0 = reinterpret_cast<float *>(srm + G::RM_PAIRS);
-    int *tabY = reinterpret_cast<int *>(sf0 + G::F0_FLOATS);
-    int *tabZ = tabY + RY;
-    int *tabYdz = tabZ + RZ;
-
+    constexpr int MZ = RG::MZ, AZ = RG::AZ, TH = TZ / 2;
     const int tz = 2 * (threadIdx.x % TH), ty = threadIdx.x / TH;
     const int x1 = min(x0 + xl, p.dx);
     const unsigned plane = (unsigned)(p.dy * p.dz);
     auto slot = [&](int q, unsigned idx) -> S * { return slots(q, idx); };
     const bool yz_fast = z_interior(p, z0, TZ) && y0 >= 1 && y0 + TY <= p.dy - 1;
-    const EosFast eos = make_eos_fast(p.eos, p.A, p.B, p.T);
-
-    for (int e = threadIdx.x; e < RY + RZ; e += NT) {
-        if (e < RY) {
-            tabY[e] = wrap_small(y0 - RH + e, p.dy);
-            tabYdz[e] = tabY[e] * p.dz;
-        } else {
-            tabZ[e - RY] = wrap_small(z0 - RH + (e - RY), p.dz);
-        }
-    }
-    __syncthreads();
-
-    auto issue_rho = [&](int xlog) {
-        const float *src = rho + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
-        float *dst = srho + (xlog & (NR - 1)) * (RY * RZ);
-        for (int e = threadIdx.x; e < RY * RZ; e += NT) {
-            const int ly = e / RZ, lz = e - ly * RZ;
-            cp_async4(dst + e, src + (unsigned)(tabYdz[ly] + tabZ[lz]));
-        }
-    };
-    // anchors: y halo 1, z halo 2 (column lz is z0 - 2 + lz)
-    auto issue_f0 = [&](int xlog) {
-        const float *src = f0c + (size_t)((unsigned)wrap_small(xlog, p.dx) * plane);
-        float *dst = sf0 + (xlog & 3) * (AY * AZ);
-        for (int e = threadIdx.x; e < AY * AZ; e += NT) {
-            const int ly = e / AZ, lz = e - ly * AZ;
-            cp_async4(dst + e, src + (unsigned)(tabYdz[ly + RH - 1] + tabZ[lz + RH - 2]));
-        }
-    };
-    auto comp_mu = [&](int xlog) {
-        const int gx = wrap_small(xlog, p.dx);
-        float2 *dst = srm + (xlog & 7) * (MY * MZ);
-        auto rpl = [&](int xx) -> const float * { return srho + (xx & (NR - 1)) * (RY * RZ); };
-        const float *rc = rpl(xlog), *rm1 = rpl(xlog - 1), *rp1 = rpl(xlog + 1);
-        const float *rm2 = rpl(xlog - 2), *rp2 = rpl(xlog + 2);
-        const float *rm3 = L == 3 ? rpl(xlog - 3) : rc;
-        const float *rp3 = L == 3 ? rpl(xlog + 3) : rc;
-        for (int e = threadIdx.x; e < MY * MZ; e += NT) {
-            const int my = e / MZ, mz = e - my * MZ;
-            const int c = (my + L) * RZ + (mz + L);
-            const float r0 = rc[c];
-            const int gz = tabZ[mz + L];
-            if (solid_k(p.wall_mode, gz, p.dz)) {
-                dst[e] = make_float2(r0, p.wall[(gz < 3 ? 0 : p.dx * p.dy) + gx * p.dy + tabY[my + L]]);
-                continue;
-            }
-            float lap;
-            if (L == 2) {
-                const float nr = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
-                const float fr = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
-                lap = fmaf(16.f, nr, fmaf(-90.f, r0, -fr)) * (1.f / 12.f);
-            } else {
-                const float n1 = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
-                const float n2 = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
-                const float n3 = (rm3[c] + rp3[c]) + (rc[c - 3 * RZ] + rc[c + 3 * RZ]) + (rc[c - 3] + rc[c + 3]);
-                lap = fmaf(270.f, n1, fmaf(-27.f, n2, fmaf(2.f, n3, -1470.f * r0))) * (1.f / 180.f);
-            }
-            dst[e] = make_float2(r0, fmaf(p.kk, mu0_fast(eos, r0), -p.ka * lap));
-        }
-    };
+    RG R(p, rho, f0c, smem4);
+    R.setup(y0, z0);
 
     const int gy = y0 + ty, gz = z0 + tz;
     const bool inA = gy < p.dy && gz < p.dz && !solid_k(p.wall_mode, gz, p.dz);
@@ -262,57 +181,29 @@ __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, cons
         for (int a = 0; a < 3; ++a) F[a] = fmaf(-gm[a], r, gr[a] * (1.0f / 3.0f));
     };
 
-    // prologue: as fused_tile
     T hv[Q - 1];
-    for (int x = x0 - 3 - L; x <= x0 - 3 + L; ++x) issue_rho(x);
-    issue_f0(x0 - 1);
-    issue_f0(x0);
-    cp_async_commit();
-    cp_async_wait_all();
-    __syncthreads();
-    comp_mu(x0 - 3);
-    for (int x = x0 - 2; x <= x0 + 2; ++x) {
-        __syncthreads();
-        issue_rho(x + L);
-        cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
-        comp_mu(x);
-    }
-    __syncthreads();
-    issue_rho(x0 + 3 + L);
-    issue_f0(x0 + 1);
-    cp_async_commit();
+    R.prologue(x0);
     fetch(x0, hv);
 
     const int mc = (ty + 3) * MZ + (tz + 3);
     const int ac = (ty + 1) * AZ + (tz + 2);  // even
     float mv2 = 0.f;  // max |MV|^2 of this thread's fluid nodes
     for (int x = x0; x < x1; ++x) {
-        cp_async_wait_all();
-        __syncthreads();
-        if (x + 1 < x1) {
-            issue_rho(x + 4 + L);
-            issue_f0(x + 2);
-        }
-        cp_async_commit();
+        R.begin_plane(x, x + 1 < x1);
         T hn[Q - 1];
         if (x + 1 < x1) fetch(x + 1, hn);
-        comp_mu(x + 3);
+        R.comp_mu(x + 3);
         __syncthreads();
         if (any) {
             const float2 *pl[7];
 #pragma unroll
-            for (int d = -3; d <= 3; ++d) pl[d + 3] = srm + ((x + d) & 7) * (MY * MZ);
+            for (int d = -3; d <= 3; ++d) pl[d + 3] = R.rm_plane(x + d);
             float rA, rB, grA[3], grB[3], FA[3], FB[3];
             force(pl, mc, rA, grA, FA);
             force(pl, mc + 1, rB, grB, FB);
             const float2 r = make_float2(rA, rB);
 
-            const float *fa[3];
-            fa[0] = sf0 + ((x - 1) & 3) * (AY * AZ);
-            fa[1] = sf0 + (x & 3) * (AY * AZ);
-            fa[2] = sf0 + ((x + 1) & 3) * (AY * AZ);
+            const float *fa[3] = {R.f0_plane(x - 1), R.f0_plane(x), R.f0_plane(x + 1)};
             const float2 a0 = *reinterpret_cast<const float2 *>(fa[1] + ac);
             float2 f[Q];
             f[0] = a0;

@@ -10,7 +10,7 @@ namespace cpmp {
 namespace fused2_detail {
 
 template <class S, int TY, int TZ, int L>
-constexpr size_t smem2() { return FusedGeom2<TY, TZ, L>::BYTES; }
+constexpr size_t smem2() { return Rings2<TY, TZ, L>::BYTES; }
 
 template <class S, int TY, int TZ, int L>
 void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, float *f0n, const float *rho,

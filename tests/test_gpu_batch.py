@@ -35,8 +35,11 @@ def test_batch_equals_individual_runs(cpmp, storage):
         ref.step(14)
         assert np.array_equal(s.get("rho"), ref.get("rho"))
         assert np.array_equal(s.get("dist"), ref.get("dist"))
-        d = s.reduce()
+        d, dr = s.reduce(), ref.reduce()
         assert d["step"] == 14 and not d["nonfinite"]
+        # the collide's per-box max |MV| (the batch keeps one slot per box and parity)
+        assert d["max_speed"] > 0 and d["max_speed"] == dr["max_speed"]
+        assert d["mass"] == dr["mass"]
         ref.close()
     b.close()
 
@@ -62,9 +65,11 @@ def test_batch_autotune_keeps_the_state(cpmp):
         s.set_flow_field(radius=box["radius"], width=4.0)
     b.step(3)
     before = [s.get("dist") for s in b.boxes]
+    speeds = [s.reduce()["max_speed"] for s in b.boxes]
     t = b.autotune()
     assert t["tile_y"] > 0 and t["step_ms"] > 0
-    for s, d in zip(b.boxes, before):
+    for s, d, v in zip(b.boxes, before, speeds):
         assert np.array_equal(s.get("dist"), d)
+        assert s.reduce()["max_speed"] == v  # the scratch steps leave the diagnostics alone
     b.step(2)
     b.close()
