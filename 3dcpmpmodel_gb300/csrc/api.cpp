@@ -1078,9 +1078,7 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
     }
     // one tile for every box: the first box's heuristic choice, refined by cpmp_batch_autotune
     b->tile = b->boxes[0]->tile;
-    int minx = b->boxes[0]->p.dx;
-    for (cpmp_handle *h : b->boxes) minx = std::min(minx, h->p.dx);
-    b->tile.xl = std::min(b->tile.xl, minx);
+    // (a march longer than a box's x extent covers that box in one chunk)
     for (cpmp_handle *h : b->boxes) h->tile = b->tile;
     cpmp_status s;
     if ((s = dalloc((void **)&b->d_params, count * sizeof(KParams<float>), "batch params")) != CPMP_OK ||
@@ -1203,7 +1201,6 @@ cpmp_status cpmp_batch_set_tile_ex(cpmp_batch *b, int tile_y, int tile_z, int ma
     if (!fused_tile_usable(b->storage, b->lap_order, tile_y, tile_z, nodes_per_thread))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
     b->tile = FusedTile{tile_y, tile_z, march_x, nodes_per_thread};
-    for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
     for (cpmp_handle *h : b->boxes) h->tile = b->tile;
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
@@ -1261,14 +1258,16 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
     cudaEventCreate(&e1);
     FusedTile best = keep;
     double best_ms = 1e30;
-    const int xls[] = {8, 16, 32, 64};
+    int maxx = 0;
+    for (cpmp_handle *h : b->boxes) maxx = std::max(maxx, h->p.dx);
+    const int xls[] = {8, 16, 32, 64, 128};
     cudaError_t err = cudaSuccess;
     for (int t = 0; t < fused_tile_count() && err == cudaSuccess; ++t) {
-        for (int xi = 0; xi < 4; ++xi) {
+        for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
             if (!fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz, ft.np)) continue;
+            if (xi > 0 && xls[xi - 1] >= maxx) continue;  // every box already in one chunk
             b->tile = ft;
-            for (cpmp_handle *h : b->boxes) b->tile.xl = std::min(b->tile.xl, h->p.dx);
             if (batch_upload(b) != CPMP_OK) break;
             batch_one_step(b, nullptr, false);
             cudaEventRecord(e0, b->st);
