@@ -213,7 +213,43 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
         const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, I) - off;
         const bool odd_off = (cz(q) & 1) != 0;
         hv[q - 1] = load_pair<S>(hp, EVEN && (P == 0 || !odd_off));
-        a[q - 1] = load_pair<float>(fI - off, EVEN && !odd_off);
+        if (!EVEN) a[q - 1] = load_pair<float>(fI - off, false);
+    }
+    if (EVEN) {
+        // anchors: in the source column (cx, cy) of the pair, direction cz
+        // needs the rest populations at z = k0 - cz and k0 + 1 - cz; the
+        // aligned pairs below k0, at k0 and above k0 + 1 hold all of them
+        auto column = [&](int ccx, int ccy, float2 &lo, float2 &mid, float2 &hi) {
+            const float *b = fI - (ccx * plane + ccy * p.dz);
+            lo = *reinterpret_cast<const float2 *>(b - 2);
+            mid = *reinterpret_cast<const float2 *>(b);
+            hi = *reinterpret_cast<const float2 *>(b + 2);
+        };
+#pragma unroll
+        for (int q = 1; q < Q; ++q) {
+            if (cz(q) != 0 || (cx(q) != 0 && cy(q) != 0)) continue;  // diagonal in-plane: below
+            if (cx(q) == 0 && cy(q) == 0) continue;
+            float2 lo, mid, hi;
+            column(cx(q), cy(q), lo, mid, hi);
+            // every q' sharing this column: cz' = 0 (this q), +1, -1
+#pragma unroll
+            for (int r2 = 1; r2 < Q; ++r2) {
+                if (cx(r2) != cx(q) || cy(r2) != cy(q)) continue;
+                a[r2 - 1] = cz(r2) == 0 ? mid : (cz(r2) == 1 ? make_float2(lo.y, mid.x) : make_float2(mid.y, hi.x));
+            }
+        }
+        {   // the pair's own column (cz = +1, -1)
+            const float2 lo = *reinterpret_cast<const float2 *>(fI - 2), hi = *reinterpret_cast<const float2 *>(fI + 2);
+            const float2 mid = *reinterpret_cast<const float2 *>(fI);
+#pragma unroll
+            for (int r2 = 1; r2 < Q; ++r2)
+                if (cx(r2) == 0 && cy(r2) == 0)
+                    a[r2 - 1] = cz(r2) == 1 ? make_float2(lo.y, mid.x) : make_float2(mid.y, hi.x);
+        }
+#pragma unroll
+        for (int q = 1; q < Q; ++q)  // in-plane diagonals: cz = 0 only
+            if (cz(q) == 0 && cx(q) != 0 && cy(q) != 0)
+                a[q - 1] = *reinterpret_cast<const float2 *>(fI - (cx(q) * plane + cy(q) * p.dz));
     }
     float2 r = *reinterpret_cast<const float2 *>(f0 + I);
 #pragma unroll
