@@ -65,15 +65,39 @@ __global__ void __launch_bounds__(kRedThreads) k_mass_partial(const uint8_t *__r
 {
     double s = 0.0, mx = 0.0;
     int bad = 0;
-    for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
-         I += (long long)gridDim.x * blockDim.x) {
-        if (type[I] != FLUID) continue;
-        const double d = (double)rho[I];
-        if (!(d >= 0.0)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
-        s += d;
-        if (mv) {
-            const double a = mv[I], b = mv[I + n], c = mv[I + 2 * n];
-            mx = fmax(mx, a * a + b * b + c * c);
+    if (sizeof(R) == 4) {
+        // FP32 fields: each thread keeps its running sum as an exact FP32
+        // pair (TwoSum: hi + lo equals the sum of the values it added up to
+        // the rounding of lo), so the FP64 pipe -- a small fraction of the
+        // FP32 rate on this part -- only joins the threads' partials; the
+        // sign test and |MV|^2 stay in FP32 as the fields are
+        float hi = 0.f, lo = 0.f, m2 = 0.f;
+        for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
+             I += (long long)gridDim.x * blockDim.x) {
+            if (type[I] != FLUID) continue;
+            const float d = (float)rho[I];
+            if (!(d >= 0.f)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
+            const float t = hi + d, bp = t - hi;
+            lo += (hi - (t - bp)) + (d - bp);
+            hi = t;
+            if (mv) {
+                const float a = (float)mv[I], b = (float)mv[I + n], c = (float)mv[I + 2 * n];
+                m2 = fmaxf(m2, fmaf(a, a, fmaf(b, b, c * c)));
+            }
+        }
+        s = (double)hi + (double)lo;
+        mx = (double)m2;
+    } else {
+        for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
+             I += (long long)gridDim.x * blockDim.x) {
+            if (type[I] != FLUID) continue;
+            const double d = (double)rho[I];
+            if (!(d >= 0.0)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
+            s += d;
+            if (mv) {
+                const double a = mv[I], b = mv[I + n], c = mv[I + 2 * n];
+                mx = fmax(mx, a * a + b * b + c * c);
+            }
         }
     }
     __shared__ double ss[kRedThreads / 32], sm[kRedThreads / 32];
