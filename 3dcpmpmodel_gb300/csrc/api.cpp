@@ -305,7 +305,7 @@ cpmp_status fused_diag_fields(cpmp_handle *h)
     CK(cudaMemsetAsync(h->mv, 0, 3 * n * sizeof(float), h->st));
     auto k = make_kparams<float>(h);
     const int P = (int)(h->step & 1);
-    plain_launch_mu_force<float>(k, h->type, (float *)h->rho, (float *)h->mu, (float *)h->F, h->st);
+    plain_launch_mu_force<float>(k, h->type, (float *)h->rho, (float *)h->mu, (float *)h->F, h->st, nullptr);
     fused_launch_velocity(h->p.storage, k, P, h->h, h->f0[P], (const float *)h->rho, (float *)h->u, h->st);
     diag_launch_mv(h->type, (const float *)h->rho, (const float *)h->u, (const float *)h->F, (float *)h->mv,
                    h->n, h->st);

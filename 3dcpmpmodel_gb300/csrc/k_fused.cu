@@ -198,7 +198,6 @@ bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np)
 
 int fused_tile_count() { return kNumTiles; }
 FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl, kTiles[idx][2]}; }
-bool fused_tile_supported(int ty, int tz, int np) { return tile_index(ty, tz, np) >= 0; }
 
 cudaError_t fused_setup_attributes()
 {

@@ -110,30 +110,6 @@ __device__ __forceinline__ void gather_pops(const KParams<float> &p, int P, cons
     }
 }
 
-// Store post-collision populations of node (i,j,k) at parity P.
-template <class S>
-__device__ __forceinline__ void scatter_pops(const KParams<float> &p, int P, S *__restrict__ h,
-                                             float *__restrict__ f0n, int i, int j, int k, long long I,
-                                             const float f[Q])
-{
-    const long long n = p.n;
-    const float a = f[0];
-    f0n[I] = a;
-#pragma unroll
-    for (int q = 1; q < Q; ++q) {
-        const S hv = f2s<S>((f[q] - ratio0(q) * a) * inv_w(q));
-        if (P == 0) {
-            h[(long long)(opp(q) - 1) * n + I] = hv;
-        } else {
-            const int di = wrap1(i + cx(q), p.dx), dj = wrap1(j + cy(q), p.dy), dk = wrap1(k + cz(q), p.dz);
-            if (solid_k(p.wall_mode, dk, p.dz))
-                h[(long long)(opp(q) - 1) * n + I] = hv;
-            else
-                h[(long long)(q - 1) * n + ((long long)di * p.dy + dj) * p.dz + dk] = hv;
-        }
-    }
-}
-
 // ------------------------------------------------------------ density ----
 // Is every node of the z-range [z0, z0+tz) and all its +-1 neighbours a fluid
 // node that needs no z wrap?

@@ -24,7 +24,7 @@ void plain_launch_macro(const KParams<R> &p, const uint8_t *type, const S *f, R 
                         cudaStream_t st);
 template <class R>
 void plain_launch_mu_force(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, R *F,
-                           cudaStream_t st, R *gm_out = nullptr);
+                           cudaStream_t st, R *gm_out);
 template <class R, class S>
 void plain_launch_step_split(const KParams<R> &p, const uint8_t *type, R *rho, R *mu, const R *u, R *F, R *mv,
                              const S *fc, S *fn, R *rho_out, R *u_out, R *gm_out, cudaStream_t st,
@@ -57,7 +57,6 @@ struct FusedTile {
 // them per grid.
 int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
-bool fused_tile_supported(int ty, int tz, int np = 1);
 // The (storage, Laplacian, tile) instantiation fits this device's shared memory.
 bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1);
 // Paired kernel (k_fused2_<storage>.cu, one unit per storage type): each
