@@ -130,3 +130,22 @@ def test_integration_cpp_binding_compiles_and_links(cpmp, tmp_path):
                         str(src), "-I", os.path.join(ROOT, "include"), "-L", libdir, "-lcpmp",
                         f"-Wl,-rpath,{libdir}", "-o", str(tmp_path / "host")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("kw,status,text", [
+    (dict(dx=0, dy=8, dz=8), 1, "grid dimensions"),
+    (dict(dx=4096, dy=4096, dz=2048), 1, "grid too large"),
+    (dict(dx=16, dy=16, dz=7, wall_mode=1), 1, "dz >= 8"),
+    (dict(dx=16, dy=16, dz=16, lap_order=9), 1, "lap_order"),
+    (dict(dx=16, dy=16, dz=16, scheme=0, storage=2), 7, "PLAIN scheme"),
+    (dict(dx=2048, dy=2048, dz=1024, scheme=1, storage=2), 7, "32 bits"),
+    (dict(dx=16, dy=16, dz=16, scheme=1, storage=0), 7, "FUSED scheme stores"),
+    (dict(dx=16, dy=16, dz=16, tau=0.5), 1, "tau"),
+])
+def test_create_rejects_invalid_parameters(cpmp, kw, status, text):
+    """cpmp_create validates the parameter set before touching the device:
+    the same errors on a machine without a GPU."""
+    p = cpmp.default_params(**kw)  # scheme 0 PLAIN / 1 FUSED; storage 0 f64, 1 f32, 2 f16, 3 bf16
+    h = C.c_void_p()
+    rc = cpmp.lib().cpmp_create(C.byref(p), C.byref(h))
+    assert rc == status and text.encode() in cpmp.lib().cpmp_last_error()
