@@ -315,7 +315,7 @@ __host__ __device__ __forceinline__ int pairs_per_column(int dz) { return (dz + 
 // rows that the same block reads, so they come from L1.
 constexpr int DENSITY_BZ = 32, DENSITY_BY = 4;
 template <class S>
-__global__ void __launch_bounds__(DENSITY_BZ *DENSITY_BY) k_density(KParams<float> p, int P,
+__global__ void __launch_bounds__(DENSITY_BZ *DENSITY_BY, 8) k_density(KParams<float> p, int P,
                                                                      const S *__restrict__ h,
                                                                      SlotTable<const S> slots,
                                                                      const float *__restrict__ f0,
