@@ -807,7 +807,7 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
 // plane's pairs (numbered column by column) in blocks of 128; blocks past a
 // box's extent exit at once.
 template <class S>
-__global__ void __launch_bounds__(128) k_density_batch(const KParams<float> *__restrict__ params,
+__global__ void __launch_bounds__(128, 8) k_density_batch(const KParams<float> *__restrict__ params,
                                                        const BatchBox *__restrict__ boxes, int P)
 {
     const int b = blockIdx.z, i = blockIdx.y;
