@@ -10,8 +10,9 @@
 // populations of the pair are one 32-bit (FP16 / BF16) or 64-bit (FP32)
 // access wherever the source or destination offset keeps that parity, two
 // scalar accesses where it does not (odd z offsets of the A-A odd step, and
-// every access of a box with an odd DZ).  Pairs next to a wall or a periodic
-// edge take a per-node general path for their global-memory accesses.
+// every access of a box with an odd DZ).  Pairs in a wall tile of an interior
+// column select their solid-source slots without wrapping; pairs at a
+// periodic edge take a per-node general path for their global accesses.
 #pragma once
 
 #include "k_fused.cuh"
@@ -57,8 +58,8 @@ struct SPair<float> {
 template <int TY, int TZ, int L>
 using Rings2 = FusedRings<TY, TZ, L, TY * TZ / 2, 2>;
 
-// One CTA owns a TY x TZ column tile and marches over xl planes of x; see
-// fused_tile for the rings and the order of work per plane.
+// One CTA owns a TY x TZ column tile and marches over xl planes of x with the
+// rings of FusedRings, in the order of work per plane of fused_tile.
 template <class S, int TY, int TZ, int L, class SL>
 __device__ __forceinline__ void fused_tile2(const KParams<float> &p, int P, const SL &slots,
                                             const float *__restrict__ f0c, float *__restrict__ f0n,
