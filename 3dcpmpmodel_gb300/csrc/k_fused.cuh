@@ -266,10 +266,38 @@ __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P
     rho[I] = r;
 }
 
+// density_wall_node for a fluid node of an x or y edge column of a walled
+// box: the sources wrap in x and y (periodic), never in z.
+template <class S, class SL>
+__device__ __forceinline__ void density_edge_node(const KParams<float> &p, int P, const SL &slots,
+                                                  const float *__restrict__ f0, float *__restrict__ rho, int i,
+                                                  int j, int k, unsigned I)
+{
+    const bool lo = k == 3, hi = k == p.dz - 4;
+    const float a0 = f0[I];
+    float hv[Q - 1], a[Q - 1];
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        const int si = wrap1(i - cx(q), p.dx), sj = wrap1(j - cy(q), p.dy);
+        const unsigned src = ((unsigned)si * p.dy + sj) * p.dz + (k - cz(q));
+        const bool ss = (cz(q) == 1 && lo) || (cz(q) == -1 && hi);
+        hv[q - 1] = s2f<S>(*((P == 0 || ss) ? slots(q - 1, I) : slots(opp(q) - 1, src)));
+        a[q - 1] = ss ? a0 : f0[src];
+    }
+    float r = a0;
+#pragma unroll
+    for (int q = 1; q < Q; ++q) {
+        r = fmaf(wgt<float>(q), hv[q - 1], r);
+        r = fmaf(ratio0(q), a[q - 1], r);
+    }
+    rho[I] = r;
+}
+
 // Density of the nodes k0 and k0 + 1 of column (i, j) (either may lie
 // outside [0, dz)); the node index of k0 is even (see pair_k0).  Pairs next
-// to a z wall in an x/y-interior column take density_wall_node, pairs at a
-// periodic edge the general per-node path.
+// to a z wall in an x/y-interior column take density_wall_node, pairs in an
+// x or y edge column of a walled box density_edge_node, pairs at a periodic
+// z edge the general per-node path.
 template <class S, class SL>
 __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, const S *__restrict__ h,
                                              const SL &slots, const float *__restrict__ f0,
@@ -283,6 +311,11 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
         if (xy && p.wall_mode == 1) {
             if (in0 && !solid_k(1, k0, p.dz)) density_wall_node<S>(p, P, slots, f0, rho, I, k0);
             if (in1 && !solid_k(1, k0 + 1, p.dz)) density_wall_node<S>(p, P, slots, f0, rho, I + 1, k0 + 1);
+            return;
+        }
+        if (p.wall_mode == 1) {
+            if (in0 && !solid_k(1, k0, p.dz)) density_edge_node<S>(p, P, slots, f0, rho, i, j, k0, I);
+            if (in1 && !solid_k(1, k0 + 1, p.dz)) density_edge_node<S>(p, P, slots, f0, rho, i, j, k0 + 1, I + 1);
             return;
         }
         if (in0) density_node<S>(p, P, h, f0, rho, i, j, k0);
