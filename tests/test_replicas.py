@@ -62,3 +62,11 @@ def test_reference_arm_nonzero_rank_exits_quietly():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "3"], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_metric_names_follow_the_scheme_and_storage():
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.metric_name(argparse.Namespace(scheme="fused", storage="f16")) == bench.METRIC
+    assert "FP32-storage plain" in bench.metric_name(argparse.Namespace(scheme="plain", storage="f32"))
