@@ -433,11 +433,15 @@ void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const
 // ------------------------------------------------- no-allocation variant ----
 // Partials of cpmp_mass_noalloc live in this file-scope device array instead
 // of a buffer the handle allocates.  Host code cannot use the array's name as
-// an address (it is a host-side stand-in); the device address is fetched with
-// cudaGetSymbolAddress once per device, with that device current, and cached.
-// Each call writes every partial triple it later reads, so nothing has to be
-// cleared between calls; calls that overlap on the GPU share the array and
-// race.
+// an address (it is a host-side stand-in); the device address comes from
+// cudaGetSymbolAddress with the device current.  It is looked up again on
+// every call made outside stream capture (the lookup allocates nothing and
+// follows the module if a device reset or a new primary context reloaded it
+// at another address); a call made while its stream is capturing uses the
+// address the last uncaptured call on that device saw, and fails if there
+// was none.  Each call writes every partial triple it later reads, so nothing
+// has to be cleared between calls; calls that overlap on the GPU share the
+// array and race.
 static __device__ __align__(256) double g_noalloc_partials[3 * kMaxRedBlocks];
 
 namespace {
@@ -445,18 +449,21 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 double *g_noalloc_addr[kMaxDevices] = {nullptr};
 
-cudaError_t noalloc_partials(double **out)
+cudaError_t noalloc_partials(cudaStream_t st, double **out)
 {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(st, &cap)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (e != cudaSuccess) return e;
+        if ((e = cudaGetSymbolAddress(&p, g_noalloc_partials)) != cudaSuccess) return e;
         g_noalloc_addr[dev] = static_cast<double *>(p);
+    } else if (!g_noalloc_addr[dev]) {
+        return cudaErrorStreamCaptureUnsupported;
     }
     *out = g_noalloc_addr[dev];
     return cudaSuccess;
@@ -478,14 +485,14 @@ extern "C" cpmp_status cpmp_mass_noalloc(const uint8_t *type, const float *rho, 
         return CPMP_ERR_SIZE;
     }
     double *part = nullptr;
-    cudaError_t e = noalloc_partials(&part);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = noalloc_partials(st, &part);
     if (e != cudaSuccess) {
         cpmp_internal_set_error((std::string("cpmp_mass_noalloc: cudaGetSymbolAddress: ") +
                                  cudaGetErrorString(e)).c_str());
         return CPMP_ERR_CUDA;
     }
     const int nb = diag_partial_blocks(n);  // <= the array's kMaxRedBlocks triples
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_mass_partial<float><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, part);
     k_mass_final<<<1, kRedThreads, 0, st>>>(part, nb, out, 1);
     e = cudaGetLastError();

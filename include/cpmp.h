@@ -337,17 +337,23 @@ void cpmp_batch_destroy(cpmp_batch *b);
  * all device pointers in the reference's node layout.  It launches on
  * `stream` (a cudaStream_t; NULL = the legacy default stream) and writes three
  * doubles to the device pointer `out`: the FP64 sum of rho over fluid nodes,
- * max |mv| (0 when mv is NULL) and 1.0 if a fluid density is NaN or negative
- * (else 0.0) -- the same deterministic reduction, in the same order, as
- * cpmp_reduce.  Its block partials live in a fixed 24 KB device array inside
- * the library (1024 partial triples; every GPU that loads the library holds
- * it until the process exits), so every n from 1 to CPMP_NOALLOC_MAX_NODES
- * fits and larger n is rejected with CPMP_ERR_SIZE.  The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress, no
- * allocation); make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU (e.g. on two streams at once)
- * race and give wrong results; each call writes every partial it reads, so
- * nothing carries over between calls that follow one another. */
+ * max |mv| over fluid nodes (0 when mv is NULL) and 1.0 if a fluid density is
+ * NaN or negative (else 0.0).  Mass and the non-finite flag are the same
+ * deterministic reduction, in the same order, as cpmp_reduce; so is max |mv|
+ * given the PLAIN scheme's MV field (the FUSED scheme's cpmp_reduce takes max
+ * |MV| from its collide kernel instead of from a field).  Its block partials
+ * live in a fixed 24 KB device array inside the library (1024 partial
+ * triples; every GPU that loads the library holds it until the process
+ * exits), so every n from 1 to CPMP_NOALLOC_MAX_NODES fits and larger n is
+ * rejected with CPMP_ERR_SIZE.  Each call outside stream capture looks up
+ * that array's device address (cudaGetSymbolAddress, no allocation), so a
+ * device reset between calls is harmless; a call on a capturing stream
+ * reuses the address of the last uncaptured call on its device and fails
+ * with CPMP_ERR_CUDA if there was none, so make one call before capturing.
+ * All calls share the array: calls that overlap on the GPU (e.g. on two
+ * streams at once) race and give wrong results; each call writes every
+ * partial it reads, so nothing carries over between calls that follow one
+ * another. */
 cpmp_status cpmp_mass_noalloc(const uint8_t *type, const float *rho, const float *mv, long long n,
                               void *stream, double *out);
 

@@ -316,6 +316,34 @@ class State:
                             C.c_double(self.den_l), out)
         return dict(zip(IMPACT_KEYS, list(out)))
 
+    def laplace(self, dens=None):
+        """Laplace-law probe of SaveDataOriDen (FluidCuda.cu:1159-1199).
+
+        Along the row (DX/2, j, DZ/2): MidDen is the mean of the densities at
+        j = 0 (outside) and j = DY/2 (inside); the radius is DY/2 minus the
+        first j in 0..DY/2 with rho(j) <= MidDen < rho(j+1), linearly
+        interpolated (0 when there is none); dp is the EOS pressure at the
+        inside probe minus that at the outside probe (EosPressure,
+        FluidCuda.cu:1561-1573, here for every EOS).  The reference scales the
+        surface tension by K (:1181); ``sigma_k`` is that value, ``sigma``
+        the one consistent with mu = K^2 mu0 (K^2 dp R / 2)."""
+        s = self.s
+        d = self.dens if dens is None else dens
+        D = lambda j: float(d[((s.dx // 2) * s.dy + j) * s.dz + s.dz // 2])  # noqa: E731
+        tout, tin = D(0), D(s.dy // 2)
+        mid = (tout + tin) / 2
+        rad = 0.0
+        for j in range(0, s.dy // 2 + 1):
+            if j + 1 >= s.dy:
+                break
+            t1, t2 = D(j), D(j + 1)
+            if t1 <= mid and t2 > mid:
+                rad = float(s.dy // 2) - (j + (mid - t1) / (t2 - t1))
+                break
+        eos = EOS_OF_MODEL[s.model]
+        dp = float(pressure(eos, self.A, self.B, self.T, tin) - pressure(eos, self.A, self.B, self.T, tout))
+        return dict(lap_r=rad, lap_dp=dp, sigma_k=s.K * dp * rad / 2, sigma=s.K * s.K * dp * rad / 2)
+
     def view(self, a):
         return a.reshape(self.s.dx, self.s.dy, self.s.dz)
 

@@ -106,3 +106,23 @@ def test_contact_angle_straight_interface(oracle_mod):
         ca = st.contact_angle(0)
         assert abs(ca["ca_left"] - theta) < 0.5, (theta, ca)
         assert abs(ca["ca_right"] - theta) < 0.5, (theta, ca)
+
+
+def test_laplace_probe_on_a_known_sphere(oracle_mod):
+    """SaveDataOriDen's radius on a tanh sphere of known radius, and its
+    pressure jump from the EOS at the two probe points."""
+    O = oracle_mod
+    s = O.Setup(dx=32, dy=48, dz=32, wall_mode=0, model=O.MP_CPCSE, tr=0.85, eos_a=0.5, eos_b=4.0)
+    dg, dl = 0.03, 0.28
+    st = O.State(s, dg, dl, "oracle")
+    i, j, k = np.meshgrid(np.arange(32), np.arange(48), np.arange(32), indexing="ij")
+    for R in (8.0, 12.5, 17.0):
+        r = np.sqrt((i - 16.0) ** 2 + (j - 24.0) ** 2 + (k - 16.0) ** 2)
+        st.dens[:] = ((dl + dg) / 2 - (dl - dg) / 2 * np.tanh((r - R) / 1.5)).reshape(-1)
+        o = st.laplace()
+        assert abs(o["lap_r"] - R) < 0.05, (R, o)
+        eos = O.EOS_OF_MODEL[s.model]
+        p_in = O.pressure(eos, st.A, st.B, st.T, st.dens[(16 * 48 + 24) * 32 + 16])
+        p_out = O.pressure(eos, st.A, st.B, st.T, st.dens[(16 * 48 + 0) * 32 + 16])
+        assert o["lap_dp"] == pytest.approx(p_in - p_out, rel=1e-14)
+        assert o["sigma"] == pytest.approx(s.K * o["sigma_k"], rel=1e-14)

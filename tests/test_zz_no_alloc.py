@@ -7,9 +7,13 @@ the entry point keeps its block partials in a fixed 24 KB device array inside
 the library.  This file is collected last so that a failure here comes after
 every other test has run; it passes alone in a fresh process as well.
 
-Checked: on two calls in a row (two different states) its three outputs equal
-those of cpmp_reduce on the same fields, to 1e-12 relative (the reductions run
-the same kernels in the same order, so they normally agree bit for bit).
+Checked, each on two calls in a row (two different states): its three
+outputs equal those of cpmp_reduce on the same PLAIN-scheme fields, to 1e-12
+relative (the reductions run the same kernels in the same order, so they
+normally agree bit for bit), on a grid that fills whole 256-node blocks and
+on one of 273 280 nodes, which is not a multiple of 256 and needs more than
+one pass of the 1024 partial blocks; without an MV field the maximum speed is
+0 and the mass unchanged.
 """
 import ctypes as C
 
@@ -19,12 +23,28 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_reduction_matches_cpmp_reduce(cpmp):
+def _call(lib, typ, rho, mv, n, out, torch):
+    out.fill_(-1.0)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.cpmp_mass_noalloc(C.c_void_p(typ.data_ptr()), C.c_void_p(rho.data_ptr()),
+                               None if mv is None else C.c_void_p(mv.data_ptr()), C.c_longlong(n),
+                               C.c_void_p(stream), C.c_void_p(out.data_ptr()))
+    assert rc == 0, lib.cpmp_last_error()
+    torch.cuda.synchronize()
+    return out.cpu().tolist()
+
+
+@pytest.mark.parametrize("dims", [(40, 16, 28), (70, 64, 61)], ids=["whole_blocks", "ragged_multipass"])
+def test_noalloc_reduction_matches_cpmp_reduce(cpmp, dims):
     torch = pytest.importorskip("torch")
     lib = cpmp.lib()
-    s = cpmp.Solver(dx=40, dy=16, dz=28, scheme=cpmp.SCHEME["plain"], storage=cpmp.STORE["f32"],
+    dx, dy, dz = dims
+    s = cpmp.Solver(dx=dx, dy=dy, dz=dz, scheme=cpmp.SCHEME["plain"], storage=cpmp.STORE["f32"],
                     base_pt=-0.04)
-    s.set_flow_field(radius=8.0, width=4.0)
+    s.set_flow_field(radius=min(dims) / 4.0, width=4.0)
+    if dims == (70, 64, 61):  # a partial last block and several nodes per thread
+        assert s.n % 256 != 0 and s.n > 1024 * 256
     out = torch.zeros(3, dtype=torch.float64, device="cuda")
     for call, steps in enumerate((5, 40)):
         s.step(steps)
@@ -33,18 +53,12 @@ def test_noalloc_reduction_matches_cpmp_reduce(cpmp):
         typ = torch.from_numpy(s.get("type")).cuda()
         rho = torch.from_numpy(s.get("rho", np.float32)).cuda()
         mv = torch.from_numpy(s.get("mv", np.float32)).cuda()
-        out.fill_(-1.0)
-        torch.cuda.synchronize()
-        stream = torch.cuda.current_stream().cuda_stream
-        rc = lib.cpmp_mass_noalloc(C.c_void_p(typ.data_ptr()), C.c_void_p(rho.data_ptr()),
-                                   C.c_void_p(mv.data_ptr()), C.c_longlong(s.n), C.c_void_p(stream),
-                                   C.c_void_p(out.data_ptr()))
-        assert rc == 0, lib.cpmp_last_error()
-        torch.cuda.synchronize()
-        mass, vmax, bad = out.cpu().tolist()
+        mass, vmax, bad = _call(lib, typ, rho, mv, s.n, out, torch)
         assert mass == pytest.approx(ref["mass"], rel=1e-12), call
         assert vmax == pytest.approx(ref["max_speed"], rel=1e-12, abs=1e-30), call
         assert bad == float(ref["nonfinite"]), call
+        mass0, vmax0, bad0 = _call(lib, typ, rho, None, s.n, out, torch)
+        assert mass0 == mass and vmax0 == 0.0 and bad0 == bad, call
     # sizes beyond the stated maximum are rejected with a clear error
     rc = lib.cpmp_mass_noalloc(C.c_void_p(typ.data_ptr()), C.c_void_p(rho.data_ptr()), None,
                                C.c_longlong((1 << 34) + 1), None, C.c_void_p(out.data_ptr()))
