@@ -5,8 +5,9 @@
 96^3 box, z walls, CS EOS (a = 0.5, b = 4) at T/Tc = 0.8, droplet radius 24
 on the bottom wall, FP32 PLAIN scheme; J = sum_fluid (rho^T - target)^2 with
 the target from a different seeded smooth 96 x 96 wall field.  Prints one
-JSON line: forward time, adjoint time (its own checkpointed forward, the
-segment replays and the reverse sweep), their ratio, the per-kernel device time
+JSON line: forward time (the PLAIN FP32 forward the adjoint differentiates,
+and the FUSED FP32 forward of the same box), adjoint time (its own
+checkpointed forward, the segment replays and the reverse sweep), the ratios, the per-kernel device time
 of a separately timed adjoint pass, and with --fd the FP64
 adjoint against central differences (h = 1e-3) for kappa and the two largest
 wall-gradient entries, plus the FP32-vs-FP64 gradient difference.
@@ -66,6 +67,24 @@ def main():
     t_fwd = e0.elapsed_time(e1) / 1e3
     s.close()
 
+    # the fastest forward the library has for this box: the FUSED scheme with
+    # FP32 storage (tile picked by the autotuner), same wall field and kappa
+    import copy
+    stf = {"params": copy.copy(st["params"]), "droplet": st["droplet"]}
+    stf["params"].scheme = cp.SCHEME["fused"]
+    s = ag._solver(stf, w0, 0.01)
+    s.autotune()
+    s.step(2)
+    s.sync()
+    stream = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = ev(enable_timing=True), ev(enable_timing=True)
+    e0.record(stream)
+    s.step(a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    t_fwd_fused = e0.elapsed_time(e1) / 1e3
+    s.close()
+
     s = ag._solver(st, w0, 0.01)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -80,6 +99,8 @@ def main():
     s.close()
     out = {"metric": "adjoint time / forward time", "value": round(t_adj / t_fwd, 3),
            "forward_s": round(t_fwd, 4), "adjoint_s": round(t_adj, 4),
+           "forward_fused_f32_s": round(t_fwd_fused, 4),
+           "adjoint_over_fused_forward": round(t_adj / t_fwd_fused, 3),
            "backward_over_forward": round((t_adj - t_fwd) / t_fwd, 3),
            "config": {"grid": [L, L, L], "steps": a.steps, "storage": "f32", "checkpoint_every": "ceil(sqrt(T))"},
            "loss": loss, "grad_kappa": gk, "grad_wall_norm": float(np.linalg.norm(gw)),

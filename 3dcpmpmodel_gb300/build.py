@@ -29,9 +29,9 @@ UNITS = [
     ("k_plain_f32.cu", []),
     ("k_plain_f64.cu", ["--fmad=false"]),
     ("k_fused.cu", ["--fmad=false"]),
-    ("k_fused2_f16.cu", ["--fmad=false"]),
-    ("k_fused2_bf16.cu", ["--fmad=false"]),
-    ("k_fused2_f32.cu", ["--fmad=false"]),
+    ("k_pair_f16.cu", ["--fmad=false"]),
+    ("k_pair_bf16.cu", ["--fmad=false"]),
+    ("k_pair_f32.cu", ["--fmad=false"]),
     ("k_diag.cu", []),
     ("k_adjoint_f32.cu", []),
     ("k_adjoint_f64.cu", ["--fmad=false"]),

@@ -30,6 +30,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 RUNNER = os.path.join(HERE, "cpmp_run")
+# wall potentials for about 30, 50, 70, 90, 110, 130 and 150 degrees in this
+# set-up, found by bisection on FUSED FP32 runs of the same box
 BASEPTS = [-0.06, -0.04, 0.02, 0.072, 0.112, 0.132, 0.15]
 
 
@@ -40,10 +42,11 @@ def coexistence():
     return co["den_g"], co["den_l"]
 
 
-def run(storage, scheme, steps, out_dir, extra=()):
+def run(storage, scheme, steps, out_dir, extra=(), basepts=None):
     cmd = [RUNNER, "--dx", "128", "--dy", "128", "--dz", "96", "--radius", "30", "--width", "5",
            "--centre", "64,64,3", "--storage", storage, "--scheme", scheme, "--allstep", str(steps),
-           "--showstep", str(steps), "--savestep", str(steps), "--basept", ",".join(map(str, BASEPTS)),
+           "--showstep", str(steps), "--savestep", str(steps),
+           "--basept", ",".join(map(str, basepts or BASEPTS)),
            "--reinit", "--out-dir", out_dir, *extra]
     t = time.perf_counter()
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -92,33 +95,57 @@ def circle_fit_angle(xz_path, den_mid, wall=2.5, above=4.0):
     return math.degrees(math.acos(c))
 
 
+def has_line(row):
+    """The reference's method found interface crossings on both sides; without
+    them its CaCap keeps the previous run's value (a global in the
+    reference), which is not reported."""
+    return row["ca_left"] != 0.0 and row["ca_right"] != 0.0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--out", default=None, help="keep the contact-angle files here")
+    ap.add_argument("--basept", default=None, help="comma-separated wall potentials (default: the calibrated seven)")
+    ap.add_argument("--only", default=None, help="one form, e.g. f32:fused, to scan wall potentials")
     a = ap.parse_args()
+    basepts = [float(v) for v in a.basept.split(",")] if a.basept else BASEPTS
     base = a.out or tempfile.mkdtemp(prefix="contact_sweep_")
+    co = coexistence()
+    mid = (co[0] + co[1]) / 2
+    if a.only:
+        storage, scheme = a.only.split(":")
+        d = os.path.join(base, f"{storage}_{scheme}")
+        os.makedirs(d, exist_ok=True)
+        rows, t = run(storage, scheme, a.steps, d, basepts=basepts)
+        for r in rows:
+            r["circle_fit"] = circle_fit_angle(os.path.join(d, "XZ_%f.txt" % r["base_pt"]), mid)
+            if not has_line(r):
+                r["ca_cap"] = None
+        print(json.dumps(dict(form=a.only, steps=a.steps, rows=rows, wall_s=t)))
+        return
     d64, d16 = os.path.join(base, "f64_plain"), os.path.join(base, "f16_fused")
     for d in (d64, d16):
         os.makedirs(d, exist_ok=True)
         for f in os.listdir(d):
             os.remove(os.path.join(d, f))
-    r64, t64 = run("f64", "plain", a.steps, d64)
-    r16, t16 = run("f16", "fused", a.steps, d16)
-    co = coexistence()
-    mid = (co[0] + co[1]) / 2
+    r64, t64 = run("f64", "plain", a.steps, d64, basepts=basepts)
+    r16, t16 = run("f16", "fused", a.steps, d16, basepts=basepts)
     per, worst, worst_fit = [], 0.0, 0.0
     for x, y in zip(r64, r16):
-        diff = {k: y[k] - x[k] for k in ("ca_left", "ca_right", "ca_cap")}
-        worst = max(worst, max(abs(v) for v in diff.values()))
+        line = has_line(x) and has_line(y)
         fit = [circle_fit_angle(os.path.join(d, "XZ_%f.txt" % x["base_pt"]), mid) for d in (d64, d16)]
+        if line:
+            diff = {k: y[k] - x[k] for k in ("ca_left", "ca_right", "ca_cap")}
+            worst = max(worst, max(abs(v) for v in diff.values()))
         if None not in fit:
             worst_fit = max(worst_fit, abs(fit[1] - fit[0]))
-        per.append(dict(base_pt=x["base_pt"], fp64=[x["ca_left"], x["ca_right"], x["ca_cap"], fit[0]],
-                        fp16=[y["ca_left"], y["ca_right"], y["ca_cap"], fit[1]]))
+        cols = lambda r: [r["ca_left"], r["ca_right"], r["ca_cap"] if line else None]  # noqa: E731
+        per.append(dict(base_pt=x["base_pt"], contact_line=line, fp64=cols(x) + [fit[0]], fp16=cols(y) + [fit[1]]))
     print(json.dumps(dict(metric="max |contact angle FP16 fused - FP64 plain|", value=worst, unit="degree",
                           circle_fit_max_diff=worst_fit, steps=a.steps, grid=[128, 128, 96], model="CP_PRW",
                           tr=0.7, radius=30, columns=["CaLeft", "CaRight", "CaCap", "circle fit"],
+                          runs_without_contact_line=sum(1 for p in per if not p["contact_line"]),
                           per_base_pt=per, wall_s=dict(f64_plain=t64, f16_fused=t16))))
 
 

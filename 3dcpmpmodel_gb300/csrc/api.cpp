@@ -61,6 +61,8 @@ struct cpmp_handle {
     unsigned *sdiag = nullptr;
     int sdiag_stride = 1;
     bool sdiag_owned = true;
+    // FUSED: error word of the collide's bounded waits (non-zero: gave up)
+    unsigned *kerr = nullptr;
     long long step = 0;
     bool initialised = false;
     std::unique_ptr<LaunchHook> hook;
@@ -120,6 +122,7 @@ KParams<R> make_kparams(const cpmp_handle *h)
     k.wall = (const R *)h->wall;
     k.mvmax = h->sdiag;
     k.mvmax_stride = h->sdiag_stride;
+    k.err = h->kerr;
     return k;
 }
 
@@ -133,6 +136,8 @@ void free_all(cpmp_handle *h)
         if (q) cudaFree(q);
     if (h->sdiag && h->sdiag_owned) cudaFree(h->sdiag);
     h->sdiag = nullptr;
+    if (h->kerr) cudaFree(h->kerr);
+    h->kerr = nullptr;
     h->type = nullptr;
     h->rho = h->rho2 = h->mu = h->u = h->mv = h->F = h->fb[0] = h->fb[1] = h->h = h->wall = nullptr;
     h->f0[0] = h->f0[1] = nullptr;
@@ -152,18 +157,24 @@ cpmp_status dalloc(void **ptr, size_t bytes, const char *what)
     return CPMP_OK;
 }
 
-// Heuristic default tile for the fused kernel (the autotuner refines it).
+// Heuristic default tile for the fused kernel (the autotuner refines it):
+// the paired kernel where the grid allows it.
 FusedTile default_tile(const cpmp_params &p)
 {
-    int ty = 8, tz = 32;
+    int ty = 8, tz = 32, np = 1;
     if (p.dy < 8) { ty = 4; tz = 32; }
     if (p.dz <= 16) { ty = p.dy < 16 ? 8 : 16; tz = 16; }
+    if (pair_grid_ok(p.dz)) {
+        np = 2;
+        ty = 8;
+        tz = p.dz > 32 ? 64 : 32;
+    }
     const long long tiles = (long long)((p.dz + tz - 1) / tz) * ((p.dy + ty - 1) / ty);
     // aim for >= 4 CTAs per SM on a 152-SM part, but march at least 8 planes
     long long xl = (long long)p.dx * tiles / (4 * 152);
     xl = std::max<long long>(8, std::min<long long>(64, xl));
     xl = std::min<long long>(xl, p.dx);
-    return FusedTile{ty, tz, (int)xl};
+    return FusedTile{ty, tz, (int)xl, np};
 }
 
 cpmp_status upload_wall(cpmp_handle *h, const std::vector<double> &w)
@@ -447,6 +458,8 @@ cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
     if (!h->plain) {
         if ((s = dalloc((void **)&h->sdiag, 2 * sizeof(unsigned), "mv max")) != CPMP_OK) return s;
         CK(cudaMemset(h->sdiag, 0, 2 * sizeof(unsigned)));
+        if ((s = dalloc((void **)&h->kerr, sizeof(unsigned), "error word")) != CPMP_OK) return s;
+        CK(cudaMemset(h->kerr, 0, sizeof(unsigned)));
     }
     if (h->plain) {
         if ((s = dalloc(&h->mu, n * rs, "mu")) != CPMP_OK) return s;
@@ -463,8 +476,9 @@ cpmp_status cpmp_create(const cpmp_params *pin, cpmp_handle **out)
         if ((s = dalloc((void **)&h->f0[1], n * sizeof(float), "f0")) != CPMP_OK) return s;
         CK(fused_setup_attributes());
         h->tile = default_tile(p);
-        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz)) h->tile = FusedTile{4, 32, h->tile.xl};
-        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz))
+        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz, h->tile.np))
+            h->tile = FusedTile{4, 32, h->tile.xl};
+        if (!fused_tile_usable(p.storage, p.lap_order, h->tile.ty, h->tile.tz, h->tile.np))
             return fail(CPMP_ERR_UNSUPPORTED, "no fused tile fits this device's shared memory");
     }
     std::vector<double> w(2 * np, p.base_pt);
@@ -574,6 +588,11 @@ cpmp_status cpmp_sync(cpmp_handle *h)
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
     CK(cudaSetDevice(h->p.device));
     CK(cudaStreamSynchronize(h->st));
+    if (h->kerr) {
+        unsigned e = 0;
+        CK(cudaMemcpy(&e, h->kerr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (e) return fail(CPMP_ERR_TIMEOUT, "fused collide: a shared-memory copy did not complete in time");
+    }
     return CPMP_OK;
 }
 
@@ -846,6 +865,7 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
         for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
             if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz, ft.np)) continue;
+            if (ft.np == 2 && !pair_grid_ok(h->p.dz)) continue;
             if (ft.xl > h->p.dx && xi > 0) continue;
             if (ft.ty > 2 * h->p.dy && ft.ty > 1) continue;
             if (ft.tz > 2 * h->p.dz) continue;
@@ -919,6 +939,8 @@ cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x
     if (nodes_per_thread != 1 && nodes_per_thread != 2) return fail(CPMP_ERR_PARAM, "nodes_per_thread must be 1 or 2");
     if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z, nodes_per_thread))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
+    if (nodes_per_thread == 2 && !pair_grid_ok(h->p.dz))
+        return fail(CPMP_ERR_UNSUPPORTED, "the paired kernel needs DZ a multiple of 4");
     h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx), nodes_per_thread};
     if (h->gexec) {
         cudaGraphExecDestroy(h->gexec);
@@ -1076,8 +1098,10 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
         h->in_batch = true;
         b->boxes.push_back(h);
     }
-    // one tile for every box: the first box's heuristic choice, refined by cpmp_batch_autotune
+    // one tile for every box: the first box's heuristic choice (one node per
+    // thread, the batched collide's form), refined by cpmp_batch_autotune
     b->tile = b->boxes[0]->tile;
+    if (b->tile.np != 1) b->tile = FusedTile{8, 32, b->tile.xl, 1};
     // (a march longer than a box's x extent covers that box in one chunk)
     for (cpmp_handle *h : b->boxes) h->tile = b->tile;
     cpmp_status s;
@@ -1197,7 +1221,7 @@ cpmp_status cpmp_batch_set_tile_ex(cpmp_batch *b, int tile_y, int tile_z, int ma
 {
     if (!b) return fail(CPMP_ERR_PARAM, "null batch");
     if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
-    if (nodes_per_thread != 1 && nodes_per_thread != 2) return fail(CPMP_ERR_PARAM, "nodes_per_thread must be 1 or 2");
+    if (nodes_per_thread != 1) return fail(CPMP_ERR_UNSUPPORTED, "batches step one node per thread");
     if (!fused_tile_usable(b->storage, b->lap_order, tile_y, tile_z, nodes_per_thread))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
     b->tile = FusedTile{tile_y, tile_z, march_x, nodes_per_thread};
@@ -1265,7 +1289,7 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
     for (int t = 0; t < fused_tile_count() && err == cudaSuccess; ++t) {
         for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
-            if (!fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz, ft.np)) continue;
+            if (ft.np != 1 || !fused_tile_usable(b->storage, b->lap_order, ft.ty, ft.tz, ft.np)) continue;
             if (xi > 0 && xls[xi - 1] >= maxx) continue;  // every box already in one chunk
             b->tile = ft;
             if (batch_upload(b) != CPMP_OK) break;

@@ -112,7 +112,7 @@ __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, con
 namespace {
 // (ty, tz, nodes per thread)
 constexpr int kTiles[][3] = {{4, 32, 1}, {8, 32, 1}, {16, 32, 1}, {16, 16, 1}, {8, 16, 1},
-                             {8, 32, 2}, {16, 32, 2}, {8, 64, 2}};
+                             {8, 32, 2}, {16, 32, 2}, {8, 64, 2}, {4, 64, 2}, {16, 64, 2}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
 template <class F>
@@ -148,11 +148,11 @@ void launch_collide_l(const KParams<float> &p, int P, const FusedTile &t, S *h, 
     else launch_collide_t<S, 8, 16, L>(p, P, t, h, f0c, f0n, rho, st);
 }
 
-bool fused2_set_attr(int storage, int lap_order, int ty, int tz, int max_smem)
+bool pair_set_attr(int storage, int lap_order, int ty, int tz, int max_smem)
 {
-    if (storage == CPMP_STORE_F16) return fused2_set_attr_f16(lap_order, ty, tz, max_smem);
-    if (storage == CPMP_STORE_BF16) return fused2_set_attr_bf16(lap_order, ty, tz, max_smem);
-    return fused2_set_attr_f32(lap_order, ty, tz, max_smem);
+    if (storage == CPMP_STORE_F16) return pair_set_attr_f16(lap_order, ty, tz, max_smem);
+    if (storage == CPMP_STORE_BF16) return pair_set_attr_bf16(lap_order, ty, tz, max_smem);
+    return pair_set_attr_f32(lap_order, ty, tz, max_smem);
 }
 
 // usable[storage index][L - 2][tile index]: the instantiation's shared
@@ -216,7 +216,7 @@ cudaError_t fused_setup_attributes()
         if (kTiles[i][2] != 2) continue;
         for (int si = 0; si < 3; ++si)
             for (int l = 0; l < 2; ++l)
-                g_usable[si][l][i] = fused2_set_attr(storages[si], l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem);
+                g_usable[si][l][i] = pair_set_attr(storages[si], l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem);
     }
     return cudaSuccess;
 }
@@ -250,11 +250,11 @@ void fused_launch_collide(int storage, const KParams<float> &p, int P, const Fus
 {
     hook_begin(hook, K_FUSED, st);
     if (t.np == 2 && storage == CPMP_STORE_F16)
-        fused2_launch_f16(p, P, t, h, f0c, f0n, rho, st);
+        pair_launch_f16(p, P, t, h, f0c, f0n, rho, st);
     else if (t.np == 2 && storage == CPMP_STORE_BF16)
-        fused2_launch_bf16(p, P, t, h, f0c, f0n, rho, st);
+        pair_launch_bf16(p, P, t, h, f0c, f0n, rho, st);
     else if (t.np == 2)
-        fused2_launch_f32(p, P, t, h, f0c, f0n, rho, st);
+        pair_launch_f32(p, P, t, h, f0c, f0n, rho, st);
     else
         with_storage(storage, [&](auto tag) {
             using S = decltype(tag);
@@ -325,20 +325,13 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     }
     hook_begin(hook, K_FUSED, st);
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    if (t.np == 2 && storage == CPMP_STORE_F16)
-        fused2_batch_f16(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
-    else if (t.np == 2 && storage == CPMP_STORE_BF16)
-        fused2_batch_bf16(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
-    else if (t.np == 2)
-        fused2_batch_f32(lap_order, t, params, boxes, nbox, total_items, P, counter, st);
-    else
-        with_storage(storage, [&](auto tag) {
-            using S = decltype(tag);
-            if (lap_order == 7)
-                batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
-            else
-                batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
-        });
+    with_storage(storage, [&](auto tag) {
+        using S = decltype(tag);
+        if (lap_order == 7)
+            batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
+        else
+            batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
+    });
     hook_end(hook, K_FUSED, st);
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {

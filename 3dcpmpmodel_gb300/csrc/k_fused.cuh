@@ -26,7 +26,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
-#include "lbm_core.cuh"
+#include "lane_math.cuh"
 #include "launch.h"
 
 namespace cpmp {
@@ -414,7 +414,7 @@ struct FusedRings {
     const KParams<float> &p;
     const float *rho, *f0c;
     unsigned plane;
-    EosFast eos;
+    EosLane eos;
     float *srho;
     float2 *srm;
     float *sf0;
@@ -424,7 +424,7 @@ struct FusedRings {
     __device__ __forceinline__ FusedRings(const KParams<float> &p_, const float *rho_, const float *f0c_,
                                           float4 *smem4)
         : p(p_), rho(rho_), f0c(f0c_), plane((unsigned)(p_.dy * p_.dz)),
-          eos(make_eos_fast(p_.eos, p_.A, p_.B, p_.T))
+          eos(make_eos_lane(p_.eos, p_.A, p_.B, p_.T))
     {
         srho = reinterpret_cast<float *>(smem4);
         srm = reinterpret_cast<float2 *>(srho + RHO_FLOATS);
@@ -508,18 +508,18 @@ struct FusedRings {
                 dst[e] = make_float2(r0, p.wall[t.y + wx]);
                 continue;
             }
-            float lap;
+            float mu;
             if (L == 2) {
-                const float nr = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
-                const float fr = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
-                lap = fmaf(16.f, nr, fmaf(-90.f, r0, -fr)) * (1.f / 12.f);
+                const float n1 = axis_sum<Lane1>(rm1[c], rp1[c], rc[c - RZ], rc[c + RZ], rc[c - 1], rc[c + 1]);
+                const float n2 = axis_sum<Lane1>(rm2[c], rp2[c], rc[c - 2 * RZ], rc[c + 2 * RZ], rc[c - 2], rc[c + 2]);
+                mu = mu_lap5<Lane1>(eos, p.kk, p.ka, r0, n1, n2);
             } else {
-                const float n1 = (rm1[c] + rp1[c]) + (rc[c - RZ] + rc[c + RZ]) + (rc[c - 1] + rc[c + 1]);
-                const float n2 = (rm2[c] + rp2[c]) + (rc[c - 2 * RZ] + rc[c + 2 * RZ]) + (rc[c - 2] + rc[c + 2]);
-                const float n3 = (rm3[c] + rp3[c]) + (rc[c - 3 * RZ] + rc[c + 3 * RZ]) + (rc[c - 3] + rc[c + 3]);
-                lap = fmaf(270.f, n1, fmaf(-27.f, n2, fmaf(2.f, n3, -1470.f * r0))) * (1.f / 180.f);
+                const float n1 = axis_sum<Lane1>(rm1[c], rp1[c], rc[c - RZ], rc[c + RZ], rc[c - 1], rc[c + 1]);
+                const float n2 = axis_sum<Lane1>(rm2[c], rp2[c], rc[c - 2 * RZ], rc[c + 2 * RZ], rc[c - 2], rc[c + 2]);
+                const float n3 = axis_sum<Lane1>(rm3[c], rp3[c], rc[c - 3 * RZ], rc[c + 3 * RZ], rc[c - 3], rc[c + 3]);
+                mu = mu_lap7<Lane1>(eos, p.kk, p.ka, r0, n1, n2, n3);
             }
-            dst[e] = make_float2(r0, fmaf(p.kk, mu0_fast(eos, r0), -p.ka * lap));
+            dst[e] = make_float2(r0, mu);
         }
     }
     // mu(x0-3 .. x0+2) evaluated; f0(x0-1 .. x0+1) and rho(x0+3+L) in flight
@@ -664,41 +664,22 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             const float2 *pl[7];
 #pragma unroll
             for (int d = -3; d <= 3; ++d) pl[d + 3] = R.rm_plane(x + d);
-            // (rho, mu) pairs: each first difference is one paired add and one
-            // paired fma per stencil distance (Blackwell FADD2 / FFMA2)
-            float2 g0 = make_float2(0.f, 0.f), g1 = g0, g2 = g0;  // (grad rho, grad mu) per axis
-            auto line = [&](int sx, int sy, int sz) -> float2 {
+            float2 lines[9];
+#pragma unroll
+            for (int l = 0; l < 9; ++l) {
                 float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int d = 1; d <= 3; ++d) {
-                    const float c = d == 1 ? 45.f : (d == 2 ? -9.f : 1.f);
-                    const int mo = sy * d * MZ + sz * d;
-                    const float2 a = pl[3 + sx * d][mc + mo], b = pl[3 - sx * d][mc - mo];
-                    acc = __ffma2_rn(make_float2(c, c), __fadd2_rn(a, make_float2(-b.x, -b.y)), acc);
+                    const int mo = line_y(l) * d * MZ + line_z(l) * d;
+                    acc = line_term(acc, line_c(d), pl[3 + line_x(l) * d][mc + mo], pl[3 - line_x(l) * d][mc - mo]);
                 }
-                return acc;
-            };
-            const float2 two = make_float2(2.f, 2.f);
-            float2 l;
-            l = line(1, 0, 0); g0 = __ffma2_rn(two, l, g0);
-            l = line(0, 1, 0); g1 = __ffma2_rn(two, l, g1);
-            l = line(0, 0, 1); g2 = __ffma2_rn(two, l, g2);
-            l = line(1, 1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, l);
-            l = line(1, -1, 0); g0 = __fadd2_rn(g0, l); g1 = __fadd2_rn(g1, make_float2(-l.x, -l.y));
-            l = line(1, 0, 1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, l);
-            l = line(1, 0, -1); g0 = __fadd2_rn(g0, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
-            l = line(0, 1, 1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, l);
-            l = line(0, 1, -1); g1 = __fadd2_rn(g1, l); g2 = __fadd2_rn(g2, make_float2(-l.x, -l.y));
-            const float inv360 = 1.0f / 360.0f;
-            const float gm[3] = {g0.y * inv360, g1.y * inv360, g2.y * inv360};
-            const float gr[3] = {g0.x * inv360, g1.x * inv360, g2.x * inv360};
+                lines[l] = acc;
+            }
             const float r = pl[3][mc].x;
-            const float Fx = fmaf(-gm[0], r, gr[0] * (1.0f / 3.0f));
-            const float Fy = fmaf(-gm[1], r, gr[1] * (1.0f / 3.0f));
-            const float Fz = fmaf(-gm[2], r, gr[2] * (1.0f / 3.0f));
+            float F[3], gr[3];
+            force_from_lines(lines, r, F, gr);
 
-            // decode with the sources' rest populations as anchors
-
+            // decode with the sources' rest populations as anchors: g = h + 3 a
             const float *fa[3] = {R.f0_plane(x - 1), R.f0_plane(x), R.f0_plane(x + 1)};
             const float a0 = fa[1][ac];
             float f[Q];
@@ -708,31 +689,17 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
                 const int sk = gz - cz(q);
                 const bool ss = !yz_fast && p.wall_mode == 1 && (sk < 3 || sk > p.dz - 4);
                 const float a = ss ? a0 : fa[1 - cx(q)][ac - cy(q) * AZ - cz(q)];
-                f[q] = fmaf(wgt<float>(q), s2f<S>(hv[q - 1]), ratio0(q) * a);
+                f[q] = fmaf(3.f, a, s2f<S>(hv[q - 1]));
             }
-            const float ir = 1.0f / r;
-            const float ux = (f[1] + f[7] + f[9] + f[11] + f[13] - f[2] - f[8] - f[10] - f[12] - f[14]) * ir;
-            const float uy = (f[3] + f[7] + f[8] + f[15] + f[17] - f[4] - f[9] - f[10] - f[16] - f[18]) * ir;
-            const float uz = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) * ir;
-            {   // MV = u + F / (2 rho), the reference's MacroCalculate velocity
-                const float hr = 0.5f * ir;
-                const float vx = fmaf(Fx, hr, ux), vy = fmaf(Fy, hr, uy), vz = fmaf(Fz, hr, uz);
-                mv2 = fmaxf(mv2, fmaf(vx, vx, fmaf(vy, vy, vz * vz)));
-            }
+            float v2;
             if (p.qp) {
                 float qp[Q];
-#pragma unroll
-                for (int a = 0; a < Q; ++a) qp[a] = 0.f;
-                qp[1] = -19.f * (p.k1 + 3.f * p.k2) * (gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
-                qp[9] = -p.k1 * (2.f * gr[0] * gr[0] - gr[1] * gr[1] - gr[2] * gr[2]);
-                qp[11] = -p.k1 * (gr[1] * gr[1] - gr[2] * gr[2]);
-                qp[13] = -p.k1 * gr[0] * gr[1];
-                qp[14] = -p.k1 * gr[2] * gr[1];
-                qp[15] = -p.k1 * gr[0] * gr[2];
-                collide_mrt_edm_fused(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, qp);
+                qp36_moments(p.k1, p.k2, gr, qp);
+                collide36<Lane1>(f, r, F[0], F[1], F[2], p.ts, p.omts, qp, v2);
             } else {
-                collide_mrt_edm_fused(f, r, ux, uy, uz, Fx, Fy, Fz, p.ts, p.omts, nullptr);
+                collide36<Lane1>(f, r, F[0], F[1], F[2], p.ts, p.omts, nullptr, v2);
             }
+            mv2 = fmaxf(mv2, v2);
 
             // encode against this node's new rest population and stream
             const int gx = wrap_small(x, p.dx);
@@ -741,19 +708,19 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             f0n[I] = an;
             if (P == 0) {
 #pragma unroll
-                for (int q = 1; q < Q; ++q) *slot(opp(q) - 1, I) = f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                for (int q = 1; q < Q; ++q) *slot(opp(q) - 1, I) = f2s<S>(fmaf(-3.f, an, f[q]));
             } else if (yz_fast && gx >= 1 && gx + 1 < p.dx) {
 #pragma unroll
                 for (int q = 1; q < Q; ++q)
                     *slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q))) =
-                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                        f2s<S>(fmaf(-3.f, an, f[q]));
             } else if (p.wall_mode == 1 && gy >= 1 && gy + 1 < p.dy && gx >= 1 && gx + 1 < p.dx) {
                 const bool lo = gz == 3, hi = gz == p.dz - 4;
 #pragma unroll
                 for (int q = 1; q < Q; ++q) {
                     const bool ss = (cz(q) == -1 && lo) || (cz(q) == 1 && hi);
                     *(ss ? slot(opp(q) - 1, I) : slot(q - 1, I + (unsigned)(cx(q) * (int)plane + cy(q) * p.dz + cz(q)))) =
-                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                        f2s<S>(fmaf(-3.f, an, f[q]));
                 }
             } else if (p.wall_mode == 1) {
                 const bool lo = gz == 3, hi = gz == p.dz - 4;
@@ -762,12 +729,12 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
                     const bool ss = (cz(q) == -1 && lo) || (cz(q) == 1 && hi);
                     const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy);
                     *(ss ? slot(opp(q) - 1, I) : slot(q - 1, (unsigned)di * plane + (unsigned)(dj * p.dz + gz + cz(q)))) =
-                        f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                        f2s<S>(fmaf(-3.f, an, f[q]));
                 }
             } else {
 #pragma unroll
                 for (int q = 1; q < Q; ++q) {
-                    const S v = f2s<S>(fmaf(-ratio0(q), an, f[q]) * inv_w(q));
+                    const S v = f2s<S>(fmaf(-3.f, an, f[q]));
                     const int di = wrap1(gx + cx(q), p.dx), dj = wrap1(gy + cy(q), p.dy), dk = wrap1(gz + cz(q), p.dz);
                     if (solid_k(p.wall_mode, dk, p.dz))
                         *slot(opp(q) - 1, I) = v;

@@ -48,7 +48,7 @@ extern template void plain_launch_mu_force<double>(const KParams<double> &, cons
 // ---- FUSED scheme (k_fused.cu) --------------------------------------------
 // storage: CPMP_STORE_F32 / F16 / BF16
 // ty x tz nodes per CTA, an x march of xl planes, np nodes per thread (1, or
-// 2 for the paired kernel of k_fused2.cu)
+// 2 for the paired kernel of k_pair.cuh)
 struct FusedTile {
     int ty, tz, xl;
     int np = 1;
@@ -59,19 +59,18 @@ int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
 // The (storage, Laplacian, tile) instantiation fits this device's shared memory.
 bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1);
-// Paired kernel (k_fused2_<storage>.cu, one unit per storage type): each
+// The paired kernel's grid requirement: DZ a multiple of 4.
+inline bool pair_grid_ok(int dz) { return dz % 4 == 0; }
+// Paired kernel (k_pair_<storage>.cu, one unit per storage type): each
 // returns false when (ty, tz) is not one of its shapes.
-#define CPMP_FUSED2_DECL(SUFFIX)                                                                                 \
-    bool fused2_set_attr_##SUFFIX(int lap_order, int ty, int tz, int max_smem);                                  \
-    bool fused2_launch_##SUFFIX(const KParams<float> &p, int P, const FusedTile &t, void *h, const float *f0c,   \
-                                float *f0n, const float *rho, cudaStream_t st);                                  \
-    bool fused2_batch_##SUFFIX(int lap_order, const FusedTile &t, const KParams<float> *params,                  \
-                               const BatchBox *boxes, int nbox, long long total, int P, unsigned *counter,       \
-                               cudaStream_t st);
-CPMP_FUSED2_DECL(f16)
-CPMP_FUSED2_DECL(bf16)
-CPMP_FUSED2_DECL(f32)
-#undef CPMP_FUSED2_DECL
+#define CPMP_PAIR_DECL(SUFFIX)                                                                                   \
+    bool pair_set_attr_##SUFFIX(int lap_order, int ty, int tz, int max_smem);                                    \
+    bool pair_launch_##SUFFIX(const KParams<float> &p, int P, const FusedTile &t, void *h, const float *f0c,     \
+                              float *f0n, const float *rho, cudaStream_t st);
+CPMP_PAIR_DECL(f16)
+CPMP_PAIR_DECL(bf16)
+CPMP_PAIR_DECL(f32)
+#undef CPMP_PAIR_DECL
 
 cudaError_t fused_setup_attributes();
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,

@@ -6,7 +6,8 @@ storage (the headline configuration; its 5.9 GB state is far larger than
 the 129 MB L2, so no L2 flush is needed between steps).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c3|c2|c1] [--storage f16|bf16|f32] [--scheme fused|plain]
+                    [--workload c3|c2|c1|c4|c3ref] [--storage f16|bf16|f32] [--scheme fused|plain]
+                    [--tile ty,tz,xl[,np]] [--profile-case X,Y,Z]
 
 Under torchrun (N > 1) every rank runs an independent replica (the step does
 not shard on one GPU per box); value is the sum over ranks, time the max.
@@ -50,11 +51,6 @@ WORKLOADS = {
                radius=30.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8,
                centre=(64.0, 64.0, 3.0)),
     "c4": dict(name="batched_96_boxes_48to112cube_fp16", batch=96, seed=0),
-    # the reference's own defaults (CP-PRW, T/Tc 0.7) on the largest cube its
-    # 32-bit population index allows (19 N < 2^31): the grid on which the
-    # reference's CUDA step is timed on this GPU as well
-    "c3ref": dict(name="reference_defaults_480cube_prw", dx=480, dy=480, dz=480, model=202, tr=0.7,
-                  radius=100.0, width=10.0, wall_mode=1, base_pt=-0.04, k=0.2, ka=0.001, tau=0.8),
     # the reference's own defaults (CP-PRW, T/Tc 0.7) on the largest cube its
     # 32-bit population index allows (19 N < 2^31): the grid on which the
     # reference's CUDA step is timed on this GPU as well
@@ -210,7 +206,13 @@ def run_ours(args) -> None:
             import torch.distributed as dist
             dist.barrier()
 
-    tile = s.autotune() if args.scheme == "fused" else None
+    tile = None
+    if args.scheme == "fused":
+        if args.tile:
+            s.set_tile(*(int(v) for v in args.tile.split(",")))
+            tile = s.tile()
+        else:
+            tile = s.autotune()
     # warm-up (includes graph capture)
     s.step(args.warmup)
     s.sync()
@@ -377,6 +379,43 @@ def run_batch(args, wl: dict, cp, torch) -> None:
     achieved = alg * b.nodes / (dom_ms / dom_launches / 1e3) / 1e9
     peaks = measured_peaks()
     bad = sum(1 for s in b.boxes if s.reduce(allow_nonfinite=True)["nonfinite"])
+
+    # ---- end to end through the public API with host buffers: every box's
+    # populations uploaded from pinned host memory (FP32), K x (one batch step
+    # + the device diagnostics of every box read back), every box's density read
+    # back to pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        cpl = cp.lib()
+        host_f = [torch.empty(Q * s.n, dtype=torch.float32, pin_memory=True).numpy() for s in b.boxes]
+        host_r = [torch.empty(s.n, dtype=torch.float32, pin_memory=True).numpy() for s in b.boxes]
+        for s, hf in zip(b.boxes, host_f):
+            cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
+                                             hf.ctypes.data_as(C.c_void_p), C.c_size_t(hf.nbytes)))
+        torch.cuda.synchronize()
+        diag = cp.Diag()
+        t0 = time.perf_counter()
+        for s, hf in zip(b.boxes, host_f):
+            cp._abi.check(cpl.cpmp_set_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
+                                             hf.ctypes.data_as(C.c_void_p), C.c_size_t(hf.nbytes)))
+        for _ in range(args.steps):
+            b.step(1)
+            for s in b.boxes:
+                rc = cpl.cpmp_reduce(s._h, C.byref(diag))
+                if rc not in (0, cp._abi.CPMP_ERR_NONFINITE):
+                    cp._abi.check(rc)
+        for s, hr in zip(b.boxes, host_r):
+            cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["rho"], cp._abi.CPMP_F32,
+                                             hr.ctypes.data_as(C.c_void_p), C.c_size_t(hr.nbytes)))
+        dt = time.perf_counter() - t0
+        e2e = {"value": round(b.nodes * args.steps / dt / 1e6, 1), "unit": "MLUPS",
+               "h2d_bytes_per_step": int(sum(h.nbytes for h in host_f) / args.steps),
+               "d2h_bytes_per_step": int((sum(h.nbytes for h in host_r) + args.steps * len(b.boxes) *
+                                          C.sizeof(cp.Diag)) / args.steps),
+               "what": "cpmp_set_field(DIST, pinned FP32) of every box + K x (cpmp_batch_step(1) + "
+                       "cpmp_reduce of every box) + cpmp_get_field(RHO, pinned FP32) of every box"}
+    cpu = None if args.no_cpu else cpu_sample(args, batch_sample_workload(wl))
     line = {
         "metric": metric_name(args) + " (aggregate over a batch)", "value": round(value, 1), "unit": "MLUPS",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -392,15 +431,18 @@ def run_batch(args, wl: dict, cp, torch) -> None:
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "peak_source": peaks["source"], "traffic": None, "alg_bytes_per_lu": alg,
                      "kernels_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in kt.items()}},
-        "e2e": None, "cpu_baseline": None,
+        "e2e": e2e, "cpu_baseline": cpu,
     }
     print(json.dumps(line))
     b.close()
 
 
-def cpu_sample(args, wl: dict) -> dict:
-    """The reference's kernels on the host cores (oracle/_ref, FP64, OpenMP),
-    or the oracle port, over a bounded sample of the workload."""
+def ref_state(args, wl: dict):
+    """The CPU reference on a bounded sample of the workload: the reference's
+    own kernels compiled for the host (oracle/_ref, FP64, OpenMP over every
+    host core) where that build exists and the workload has the reference's
+    z walls, else the oracle port; the grid is halved along its longest axis
+    until it holds at most --cpu-nodes nodes.  Returns (state, kind, grid)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
@@ -412,7 +454,6 @@ def cpu_sample(args, wl: dict) -> dict:
         kind = "port"
     if wl["wall_mode"] != 1:
         kind = "port"  # the reference step always has z walls
-    # bounded sample: same physics, grid capped so a step takes seconds
     dx, dy, dz = wl["dx"], wl["dy"], wl["dz"]
     cap = args.cpu_nodes
     while dx * dy * dz > cap:
@@ -436,6 +477,29 @@ def cpu_sample(args, wl: dict) -> dict:
     s = O.Setup(**kw)
     g, l = O.coexistence(model, tr, s.eos_a, s.eos_b)
     st = O.State(s, g, l, "ref" if kind == "reference" else "oracle").init()
+    return st, kind, (dx, dy, dz)
+
+
+def host_cores() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def cpu_model() -> str:
+    """The host CPU's model name as lscpu reports it ("" if unavailable)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        return ""
+    for line in out.splitlines():
+        if line.startswith("Model name:"):
+            return line.split(":", 1)[1].strip()
+    return ""
+
+
+def cpu_sample(args, wl: dict) -> dict:
+    """cpu_baseline: the CPU reference (ref_state) stepped for about
+    --cpu-seconds after one warm-up step."""
+    st, kind, (dx, dy, dz) = ref_state(args, wl)
     st.step(1)
     steps = 0
     t0 = time.perf_counter()
@@ -445,9 +509,9 @@ def cpu_sample(args, wl: dict) -> dict:
         if time.perf_counter() - t0 > args.cpu_seconds:
             break
     dt = time.perf_counter() - t0
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return {"value": round(dx * dy * dz * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": cores,
-            "kind": kind, "sample": f"{steps} steps of a {dx}x{dy}x{dz} box, same EOS/T/walls, FP64"}
+    return {"value": round(dx * dy * dz * steps / dt / 1e6, 3), "unit": "MLUPS", "cores": host_cores(),
+            "cpu": cpu_model(), "kind": kind,
+            "sample": f"{steps} steps of a {dx}x{dy}x{dz} box, same EOS/T/walls, FP64"}
 
 
 def batch_sample_workload(wl: dict) -> dict:
@@ -463,30 +527,51 @@ def batch_sample_workload(wl: dict) -> dict:
 
 
 def run_reference(args) -> None:
+    """The reference arm: the CPU reference (ref_state) on every host core,
+    W untimed warm-up steps, then K timed steps of the bounded sample."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
     wl = WORKLOADS[args.workload]
     if "batch" in wl:
         wl = batch_sample_workload(wl)
-    for _ in range(args.warmup):
-        pass
-    samples = []
-    cpu = None
-    for _ in range(max(1, min(args.steps, args.ref_repeats))):
-        cpu = cpu_sample(args, wl)
-        samples.append(cpu["value"])
-    v = statistics.median(samples)
-    cpu["value"] = v
+    st, kind, (dx, dy, dz) = ref_state(args, wl)
+    st.step(args.warmup)
+    t0 = time.perf_counter()
+    st.step(args.steps)
+    dt = time.perf_counter() - t0
+    v = round(dx * dy * dz * args.steps / dt / 1e6, 3)
+    cpu = {"value": v, "unit": "MLUPS", "cores": host_cores(), "cpu": cpu_model(), "kind": kind,
+           "sample": f"{args.steps} steps of a {dx}x{dy}x{dz} box, same EOS/T/walls, FP64"}
     line = {"metric": metric_name(args), "value": v, "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded droplet initial field, no dataset)",
             "config": {"workload": wl["name"], "grid": [wl["dx"], wl["dy"], wl["dz"]],
-                       "parallelism": "host cores"},
+                       "sample_grid": [dx, dy, dz], "parallelism": "host cores"},
             "impl": "reference", "cpu_baseline": cpu,
             "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def run_profile_case(args) -> None:
+    """A few steps of one box with the workload's physics on a grid of
+    --profile-case, for profilers (no timing, no CPU leg); prints the mass."""
+    import importlib
+    importlib.import_module("3dcpmpmodel_gb300.build").build()
+    cp = importlib.import_module("3dcpmpmodel_gb300")
+    wl = dict(WORKLOADS[args.workload])
+    wl["dx"], wl["dy"], wl["dz"] = (int(v) for v in args.profile_case.split(","))
+    wl["radius"] = min(wl["radius"], wl["dz"] / 3)
+    wl.pop("centre", None)
+    s = make_solver(cp, wl, args.scheme, args.storage, 0)
+    if args.tile and args.scheme == "fused":
+        s.set_tile(*(int(v) for v in args.tile.split(",")))
+    s.step(args.steps)
+    s.sync()
+    print(json.dumps({"profile_case": [wl["dx"], wl["dy"], wl["dz"]], "steps": args.steps,
+                      "tile": s.tile() if args.scheme == "fused" else None, "mass": s.reduce()["mass"]}))
+    s.close()
 
 
 def main():
@@ -500,10 +585,16 @@ def main():
     ap.add_argument("--storage", choices=["f16", "bf16", "f32", "f64"], default="f16")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--cpu-nodes", type=int, default=2_000_000)
-    ap.add_argument("--ref-repeats", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tile", default="", help="ty,tz,xl[,np]: this fused tile instead of the autotuner's")
+    ap.add_argument("--profile-case", default="",
+                    help="X,Y,Z: only run --steps steps of a box of this grid with the workload's physics "
+                         "(for profilers; no timing)")
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":

@@ -12,9 +12,10 @@ TEST INFRASTRUCTURE ONLY.  Generates, into oracle/_ref/ (git-ignored):
 
 and compiles ``oracle/ref_shim.cpp`` against them into ``oracle/_ref/libref.so``.
 
-Generation needs the reference tree (``--src``, default the mounted
-reference); compiling needs only the generated files, so a machine without
-the reference tree can still build the library from a copied ``_ref/``.
+Generation needs the reference tree (``--src`` or the CPMP_REFERENCE_SRC
+environment variable); compiling needs only the generated files, so a machine
+without the reference tree can still build the library from a copied
+``_ref/``.
 """
 import argparse
 import os
@@ -24,7 +25,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_SRC = "/root/reference"
+# location of the reference tree: --src, or the CPMP_REFERENCE_SRC environment
+# variable; without either, only an existing generated copy is compiled
+DEFAULT_SRC = os.environ.get("CPMP_REFERENCE_SRC", "")
 
 GRID_LINES = {  # Common.h line (1-based) -> expected declaration prefix
     25: "const int DY",
@@ -109,7 +112,7 @@ def compile_lib() -> str:
 def build_tecplot(src: str = DEFAULT_SRC) -> str | None:
     """The reference's Tecplot writer (ordered_tec.cpp, compiled from the
     reference tree where it lies) behind oracle/tec_ref_driver.cpp."""
-    if not os.path.isfile(os.path.join(src, "ordered_tec.cpp")):
+    if not src or not os.path.isfile(os.path.join(src, "ordered_tec.cpp")):
         return None
     os.makedirs(OUT, exist_ok=True)
     out = os.path.join(OUT, "libtecref.so")
@@ -122,7 +125,7 @@ def build_tecplot(src: str = DEFAULT_SRC) -> str | None:
 def build(src: str = DEFAULT_SRC) -> str | None:
     """Generate (when the reference tree exists) and compile; returns the .so
     path, or None when neither the reference tree nor generated files exist."""
-    if os.path.isfile(os.path.join(src, "FluidCuda.cu")):
+    if src and os.path.isfile(os.path.join(src, "FluidCuda.cu")):
         generate(src)
         generate_gpu(src)
     if not (os.path.isfile(os.path.join(OUT, "Common_rt.h"))

@@ -1,8 +1,10 @@
 """Generate the committed golden fixtures from the reference itself.
 
-Run in a container that has the reference tree (default /root/reference):
+Run where the reference tree is present, giving its location:
 
-    python tests/golden/make_golden.py [--src /root/reference]
+    python tests/golden/make_golden.py --src <reference tree>
+
+(or set CPMP_REFERENCE_SRC to that location).
 
 Writes into tests/golden/:
   * cocurve_rows.json  -- rows of the reference's CoCurve_<EOS>_2.txt tables
@@ -143,7 +145,7 @@ def write_tecplot_golden():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", default=os.environ.get("CPMP_REFERENCE_SRC"), required="CPMP_REFERENCE_SRC" not in os.environ)
     a = ap.parse_args()
     if O.build_ref() is None:
         sys.exit("oracle/_ref could not be built (reference sources unavailable)")

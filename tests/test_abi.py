@@ -115,19 +115,17 @@ def test_create_without_gpu_fails_cleanly(cpmp):
 
 
 def test_integration_cpp_binding_compiles_and_links(cpmp, tmp_path):
-    """The C++ binding a maintainer of the reference would add (the cpp block of
-    INTEGRATION.md) compiles against include/cpmp.h and links to libcpmp.so,
-    with the reference's compile-time grid and step counts as macros."""
+    """The C++ binding a maintainer of the reference would add
+    (csrc/reference_host_binding.cpp) compiles against include/cpmp.h and links
+    to libcpmp.so, with the reference's compile-time grid and step counts as
+    macros."""
     import shutil
     if not shutil.which("g++"):
         pytest.skip("no host C++ compiler")
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    code = re.search(r"```cpp\n(.*?)```", text, re.S).group(1)
-    src = tmp_path / "host.cpp"
-    src.write_text("#include <cstdio>\n" + code)
+    src = os.path.join(ROOT, "3dcpmpmodel_gb300", "csrc", "reference_host_binding.cpp")
     libdir = os.path.join(ROOT, "3dcpmpmodel_gb300")
     r = subprocess.run(["g++", "-O1", "-DDX=64", "-DDY=64", "-DDZ=64", "-DAllStep=100", "-DShowStep=10",
-                        str(src), "-I", os.path.join(ROOT, "include"), "-L", libdir, "-lcpmp",
+                        src, "-I", os.path.join(ROOT, "include"), "-L", libdir, "-lcpmp",
                         f"-Wl,-rpath,{libdir}", "-o", str(tmp_path / "host")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 

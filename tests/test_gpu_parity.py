@@ -191,19 +191,20 @@ def test_fused_result_is_independent_of_tile(cpmp, storage):
 
 
 @pytest.mark.parametrize("cfg", [
-    dict(dx=20, dy=18, dz=37, radius=7.0, width=4.0, base_pt=-0.04),                      # odd DZ, walls
-    dict(dx=24, dy=20, dz=30, radius=6.0, width=3.0, wall_mode=0, centre=(12, 10, 15)),   # periodic
-    dict(dx=20, dy=18, dz=26, radius=6.0, width=4.0, base_pt=0.02, K1=0.002, K2=-0.002, tau=1.0,
+    dict(dx=20, dy=18, dz=36, radius=7.0, width=4.0, base_pt=-0.04),                      # walls, partial z tile
+    dict(dx=24, dy=20, dz=32, radius=6.0, width=3.0, wall_mode=0, centre=(12, 10, 15)),   # periodic edges
+    dict(dx=20, dy=18, dz=28, radius=6.0, width=4.0, base_pt=0.02, K1=0.002, K2=-0.002, tau=1.0,
          lap_order=7),                                                                    # K1/K2, 7-point
-], ids=["odd_dz", "periodic", "k1k2_lap7"])
+], ids=["walls", "periodic", "k1k2_lap7"])
 @pytest.mark.parametrize("storage", ["f16", "bf16", "f32"])
 def test_paired_kernel_matches_single_node_kernel(cpmp, cfg, storage):
-    """Two nodes per thread (paired FP32 instructions) give exactly the bits
-    of one node per thread, on every global-access path: odd DZ (no paired
-    accesses), periodic edges, walls, the K1/K2 term and the 7-point
-    Laplacian."""
+    """Two nodes per thread (paired FP32 instructions, bulk-copy rings) give
+    exactly the bits of one node per thread, on every access path: walls,
+    periodic x / y / z edges (wrapped ring rows and index corrections), tiles
+    reaching past the box, the K1/K2 term and the 7-point Laplacian."""
     runs = []
-    for ty, tz, xl, npt in ((8, 32, 9, 1), (8, 32, 9, 2), (16, 32, 5, 2), (8, 64, 64, 2)):
+    for ty, tz, xl, npt in ((8, 32, 9, 1), (8, 32, 9, 2), (16, 32, 5, 2), (8, 64, 64, 2), (4, 64, 7, 2),
+                            (16, 64, 11, 2)):
         s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
         s.set_tile(ty, tz, xl, npt)
         s.step(11)
@@ -213,6 +214,17 @@ def test_paired_kernel_matches_single_node_kernel(cpmp, cfg, storage):
     for r, d in runs[1:]:
         assert np.array_equal(r, runs[0][0])
         assert np.array_equal(d, runs[0][1])
+
+
+def test_paired_kernel_needs_dz_multiple_of_four(cpmp):
+    s = solver_for(cpmp, dict(dx=20, dy=18, dz=37, radius=7.0, width=4.0), scheme="fused", storage="f16")
+    with pytest.raises(cpmp.CpmpError) as e:
+        s.set_tile(8, 32, 9, 2)
+    assert e.value.status == 7
+    s.set_tile(8, 32, 9, 1)
+    s.step(3)
+    assert np.isfinite(s.get("rho")).all()
+    s.close()
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
