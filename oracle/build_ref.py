@@ -25,9 +25,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-# location of the reference tree: --src, or the CPMP_REFERENCE_SRC environment
-# variable; without either, only an existing generated copy is compiled
-DEFAULT_SRC = os.environ.get("CPMP_REFERENCE_SRC", "")
+# location of the reference tree: --src, the CPMP_REFERENCE_SRC environment
+# variable, or the read-only mount this recipe reads it from; where none of
+# them holds the tree, only an existing generated copy is compiled
+DEFAULT_SRC = os.environ.get("CPMP_REFERENCE_SRC") or "/root/reference"
 
 GRID_LINES = {  # Common.h line (1-based) -> expected declaration prefix
     25: "const int DY",
