@@ -119,9 +119,10 @@ __device__ __forceinline__ bool z_interior(const KParams<float> &p, int z0, int 
 }
 
 // rho = sum of the post-stream populations (MacroCalculate's density,
-// FluidCuda.cu:357-361) on fluid nodes: r = f0, then r += f_q for q = 1..18
-// in order, each term decoded by decode_pop.  The general path, for nodes
-// next to a wall or a periodic edge.
+// FluidCuda.cu:357-361) on fluid nodes, in the collision's scaled form: each
+// population decoded as g = h + 3 a (the collide's decode), rho = f_0 +
+// (2 ES + DS) / 36 (mass_sums, correctly rounded division).  The general path,
+// for nodes next to a wall or a periodic edge.
 template <class S>
 __device__ __forceinline__ void density_node(const KParams<float> &p, int P, const S *__restrict__ h,
                                              const float *__restrict__ f0, float *__restrict__ rho, int i, int j,
@@ -129,12 +130,21 @@ __device__ __forceinline__ void density_node(const KParams<float> &p, int P, con
 {
     if (solid_k(p.wall_mode, k, p.dz)) return;
     const long long I = ((long long)i * p.dy + j) * p.dz + k;
-    float f[Q];
-    gather_pops<S>(p, P, h, f0, i, j, k, I, f);
-    float r = f[0];
+    const long long n = p.n;
+    const float a0 = f0[I];
+    float g[Q];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) r = __fadd_rn(r, f[q]);
-    rho[I] = r;
+    for (int q = 1; q < Q; ++q) {
+        const int si = wrap1(i - cx(q), p.dx), sj = wrap1(j - cy(q), p.dy), sk = wrap1(k - cz(q), p.dz);
+        const bool ss = solid_k(p.wall_mode, sk, p.dz);
+        const long long src = ((long long)si * p.dy + sj) * p.dz + sk;
+        const float a = ss ? a0 : __ldg(f0 + src);
+        const float hv = s2f<S>((P == 0 || ss) ? h[(long long)(q - 1) * n + I] : h[(long long)(opp(q) - 1) * n + src]);
+        g[q] = fmaf(3.f, a, hv);
+    }
+    float ES, DS;
+    mass_sums<Lane1>(g, ES, DS);
+    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
 }
 
 // Two stored values of consecutive nodes as a float pair: one vector load
@@ -165,8 +175,8 @@ __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
     return p.wall_mode == 1 ? (k >= 4 && k <= p.dz - 5) : (k >= 1 && k <= p.dz - 2);
 }
 
-// Paired density of nodes I and I + 1 (I even, both with plain sources):
-// r += w_q h_q, then r += (w_q / w_0) a_q, q in order, in paired FP32.  With
+// Paired density of nodes I and I + 1 (I even, both with plain sources), in
+// paired FP32 (the sums of density_node).  With
 // an even DZ every pair of loads has a parity known at compile time (node
 // index and N even, so it is that of cz(q)) and aligned pairs are vector
 // loads; otherwise all moving-population and anchor loads are scalar.  Every
@@ -227,19 +237,17 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
             if (cz(q) == 0 && cx(q) != 0 && cy(q) != 0)
                 a[q - 1] = *reinterpret_cast<const float2 *>(fI - (cx(q) * plane + cy(q) * p.dz));
     }
-    float2 r = *reinterpret_cast<const float2 *>(f0 + I);
+    float2 g[Q];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) {
-        const float w = wgt<float>(q), rw = ratio0(q);
-        r = __ffma2_rn(make_float2(w, w), hv[q - 1], r);
-        r = __ffma2_rn(make_float2(rw, rw), a[q - 1], r);
-    }
-    *reinterpret_cast<float2 *>(rho + I) = r;
+    for (int q = 1; q < Q; ++q) g[q] = Lane2::fma(Lane2::k(3.f), a[q - 1], hv[q - 1]);
+    float2 ES, DS;
+    mass_sums<Lane2>(g, ES, DS);
+    const float2 a0 = *reinterpret_cast<const float2 *>(f0 + I);
+    *reinterpret_cast<float2 *>(rho + I) = Lane2::add(a0, Lane2::div_rn(Lane2::fma(Lane2::k(2.f), ES, DS), 36.f));
 }
 
 // Density of one fluid node k of an x/y-interior column of a walled box
-// (wall_mode 1): the paired path's sums (r += w_q h_q, then r += (w_q / w_0)
-// a_q, q in order, fused multiply-adds) with each source across the wall
+// (wall_mode 1): the sums of density_node with each source across the wall
 // layer (k = 3 or dz - 4) replaced by the node's own slot and rest population.
 template <class S, class SL>
 __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P, const SL &slots,
@@ -257,13 +265,12 @@ __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P
         hv[q - 1] = s2f<S>(*((P == 0 || ss) ? slots(q - 1, I) : slots(opp(q) - 1, src)));
         a[q - 1] = ss ? a0 : f0[src];
     }
-    float r = a0;
+    float g[Q];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) {
-        r = fmaf(wgt<float>(q), hv[q - 1], r);
-        r = fmaf(ratio0(q), a[q - 1], r);
-    }
-    rho[I] = r;
+    for (int q = 1; q < Q; ++q) g[q] = fmaf(3.f, a[q - 1], hv[q - 1]);
+    float ES, DS;
+    mass_sums<Lane1>(g, ES, DS);
+    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
 }
 
 // density_wall_node for a fluid node of an x or y edge column of a walled
@@ -284,13 +291,12 @@ __device__ __forceinline__ void density_edge_node(const KParams<float> &p, int P
         hv[q - 1] = s2f<S>(*((P == 0 || ss) ? slots(q - 1, I) : slots(opp(q) - 1, src)));
         a[q - 1] = ss ? a0 : f0[src];
     }
-    float r = a0;
+    float g[Q];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) {
-        r = fmaf(wgt<float>(q), hv[q - 1], r);
-        r = fmaf(ratio0(q), a[q - 1], r);
-    }
-    rho[I] = r;
+    for (int q = 1; q < Q; ++q) g[q] = fmaf(3.f, a[q - 1], hv[q - 1]);
+    float ES, DS;
+    mass_sums<Lane1>(g, ES, DS);
+    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
 }
 
 // Density of the nodes k0 and k0 + 1 of column (i, j) (either may lie

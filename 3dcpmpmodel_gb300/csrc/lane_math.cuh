@@ -39,6 +39,7 @@ struct Lane1 {
     static __device__ __forceinline__ V rcp(V a) { return __fdividef(1.0f, a); }
     static __device__ __forceinline__ V lg2(V a) { return __log2f(a); }
     static __device__ __forceinline__ V rcp_rn(V a) { return __frcp_rn(a); }
+    static __device__ __forceinline__ V div_rn(V a, float d) { return __fdiv_rn(a, d); }
 };
 
 struct Lane2 {
@@ -57,6 +58,7 @@ struct Lane2 {
     static __device__ __forceinline__ V rcp(V a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
     static __device__ __forceinline__ V lg2(V a) { return make_float2(__log2f(a.x), __log2f(a.y)); }
     static __device__ __forceinline__ V rcp_rn(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+    static __device__ __forceinline__ V div_rn(V a, float d) { return make_float2(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d)); }
 };
 
 // ---------------------------------------------------------------- EOS ----
@@ -240,6 +242,21 @@ __device__ __forceinline__ void moments36(const typename O::V g[Q], typename O::
     m[18] = O::sub(ZXZ, ZYZ);
 }
 
+// Mass of a node's populations in the scaled form: sum_q f_q = f_0 + (2 ES +
+// DS) / 36 with ES the sum of g over the six axis directions and DS over the
+// twelve diagonal ones.  Both the collision (the rest population as the
+// remainder of the new mass) and the density pass use these sums and a
+// correctly rounded division by 36, so no rounded weight enters the mass
+// balance: the lattice mass then changes only by unbiased roundings.
+template <class O>
+__device__ __forceinline__ void mass_sums(const typename O::V g[Q], typename O::V &ES, typename O::V &DS)
+{
+    ES = O::add(O::add(O::add(g[1], g[2]), O::add(g[3], g[4])), O::add(g[5], g[6]));
+    DS = O::add(O::add(O::add(O::add(g[7], g[8]), O::add(g[9], g[10])),
+                       O::add(O::add(g[11], g[12]), O::add(g[13], g[14]))),
+                O::add(O::add(g[15], g[16]), O::add(g[17], g[18])));
+}
+
 // 36 meq(rho, u) given r36 = 36 rho (moments 16..18 vanish)
 template <class O>
 __device__ __forceinline__ void meq36(typename O::V r36, typename O::V ux, typename O::V uy, typename O::V uz,
@@ -365,6 +382,11 @@ __device__ __forceinline__ void collide36(typename O::V g[Q], typename O::V rho,
         m[a] = v;
     }
     inverse36<O>(m, g);
+    // rest population: the remainder of the relaxed mass moment 36 rho*, so the
+    // node emits exactly (up to the last rounding) the mass it keeps
+    V ES, DS;
+    mass_sums<O>(g, ES, DS);
+    g[0] = O::div_rn(O::sub(m[0], O::fma(O::k(2.f), ES, DS)), 36.f);
 }
 
 // 36 x the K1/K2 pressure-tensor moments Qp (FluidCuda.cu:260-266) from

@@ -99,15 +99,19 @@ def test_laplace_probe_matches_oracle(cpmp, oracle_mod, cfg):
 
 
 # Measured maximum relative errors of FP32 runs against the FP64 reference
-# (walled CP-PRW box below) grow about linearly with the step count -- FP32
-# rounding in a near-steady state repeats the same way every step:
+# (walled CP-PRW box below):
 #   steps          10       100      200      500      1000
 #   PLAIN rho    5.9e-7   1.7e-6   3.6e-6   8.3e-6   1.8e-5
-#   FUSED rho    1.4e-6   1.0e-5   2.2e-5   2.8e-5   3.7e-5
-# so the 1e-5 bound is met to about 500 steps by the plain scheme and to
-# about 100 by the fused one; after 1000 steps the bounds asserted are those
-# of the measured curve with a 1.6x margin.
-FP32_1000 = {"plain": (3e-5, 2e-5), "fused": (6e-5, 4e-5)}
+#   FUSED rho    1.2e-6   9.5e-6   1.9e-5   2.5e-5   2.9e-5
+#   FUSED u      2.2e-6   8.5e-6   5.4e-6   7.0e-6   8.8e-6
+# The plain scheme (the reference's operator sequence in FP32) drifts about
+# linearly; the fused scheme balances mass without a rounded weight (each
+# node's rest population is the remainder of its new density, the density
+# pass divides by 36 with correct rounding), so its error levels off.  The
+# 1e-5 bound holds to about 500 steps (plain) and 100 steps (fused); after
+# 1000 steps the bounds asserted are those of the measured curve with a
+# margin of about 1.5.
+FP32_1000 = {"plain": (3e-5, 2e-5), "fused": (4.5e-5, 2e-5)}
 
 
 @pytest.mark.parametrize("scheme", ["plain", "fused"])
