@@ -34,9 +34,9 @@ def smooth_field(nx, ny, seed, amp, mean=0.0, corr=8.0):
     return mean + amp * w
 
 
-def setup(storage, L=96, radius=24.0):
+def setup(storage, L=96, radius=24.0, scheme="plain"):
     p = cp.default_params(dx=L, dy=L, dz=L, model=206, tr=0.8, eos_a=0.5, eos_b=4.0, ka=0.01, tau=1.0,
-                          base_pt=0.0, scheme=cp.SCHEME["plain"], storage=cp.STORE[storage])
+                          base_pt=0.0, scheme=cp.SCHEME[scheme], storage=cp.STORE[storage])
     return {"params": p, "droplet": dict(radius=radius, width=4.0, centre=(L / 2, L / 2, 3.0))}
 
 
@@ -69,9 +69,7 @@ def main():
 
     # the fastest forward the library has for this box: the FUSED scheme with
     # FP32 storage (tile picked by the autotuner), same wall field and kappa
-    import copy
-    stf = {"params": copy.copy(st["params"]), "droplet": st["droplet"]}
-    stf["params"].scheme = cp.SCHEME["fused"]
+    stf = setup("f32", L, L / 4, scheme="fused")
     s = ag._solver(stf, w0, 0.01)
     s.autotune()
     s.step(2)

@@ -5,8 +5,8 @@
 128 x 128 x 96 box with z walls, CP-PRW at T/Tc = 0.7 (the reference's
 Initialize() defaults otherwise), a hemispherical droplet of radius 30
 centred on the first fluid layer (64, 64, 3), and seven wall potentials
-spanning about 30 to 150 degrees from the reference's calibration list
-(FluidCuda.cu:128).  Each BasePt starts from a fresh droplet and runs
+spanning about 30 to 150 degrees in this set-up (the reference's calibration
+list, FluidCuda.cu:128, is for another droplet size).  Each BasePt starts from a fresh droplet and runs
 `--steps` steps through cpmp_run, the driver with the reference's host loop;
 the contact angles are read back from the SaveContactAngle files the two runs
 write.  The reference's method needs an interface crossing in the solid row
@@ -31,8 +31,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 RUNNER = os.path.join(HERE, "cpmp_run")
 # wall potentials for about 30, 50, 70, 90, 110, 130 and 150 degrees in this
-# set-up, found by bisection on FUSED FP32 runs of the same box
-BASEPTS = [-0.06, -0.04, 0.02, 0.072, 0.112, 0.132, 0.15]
+# set-up (spherical-cap angle), picked from a scan of FUSED FP32 runs of the
+# same box over -0.055 .. 0.105 (below -0.05 the droplet spreads into a film,
+# from 0.1 it leaves the wall)
+BASEPTS = [-0.044, -0.03, -0.01, 0.01, 0.037, 0.063, 0.09]
 
 
 def coexistence():

@@ -261,9 +261,19 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
     auto comp_mu = [&](int pl) {
         const int gx = wrap_small(pl, p.dx);
         float2 *dst = rm_plane(pl);
-        const float *rc = rho_plane(pl), *rm1 = rho_plane(pl - 1), *rp1 = rho_plane(pl + 1);
-        const float *rm2 = rho_plane(pl - 2), *rp2 = rho_plane(pl + 2);
-        const float *rm3 = L == 3 ? rho_plane(pl - 3) : rc, *rp3 = L == 3 ? rho_plane(pl + 3) : rc;
+        // planes pl-L .. pl+L: one slot computation, then consecutive slots
+        const float *rpl[2 * L + 1];
+        {
+            int sl = rslot(pl - L);
+#pragma unroll
+            for (int k = 0; k <= 2 * L; ++k) {
+                rpl[k] = srho + sl * (RY * RZ);
+                sl = sl + 1 == NR ? 0 : sl + 1;
+            }
+        }
+        const float *rc = rpl[L], *rm1 = rpl[L - 1], *rp1 = rpl[L + 1];
+        const float *rm2 = rpl[L - 2], *rp2 = rpl[L + 2];
+        const float *rm3 = L == 3 ? rpl[0] : rc, *rp3 = L == 3 ? rpl[2 * L] : rc;
         auto ld = [](const float *b, int i) { return *reinterpret_cast<const float2 *>(b + i); };
 #pragma unroll
         for (int k = 0; k < RG::KM; ++k) {
@@ -336,9 +346,14 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
                 v = *reinterpret_cast<const T *>(b + src);
             } else {
                 const unsigned ca = (edge && cz(q) == 1) ? zsA : 0u, cb = (edge && cz(q) == -1) ? zsB : 0u;
-                v = SP::make(b[src + ca], b[src + 1u + cb]);
-                if (cz(q) == 1 && botw) v = *reinterpret_cast<const T *>(slot(q - 1, I));
-                if (cz(q) == -1 && topw) v = *reinterpret_cast<const T *>(slot(q - 1, I));
+                // a source on a wall layer: the node's own slot (half-way
+                // bounce-back) -- node B of (2, 3) for cz = +1, node A of
+                // (dz-4, dz-3) for cz = -1; selected addresses, no branch
+                const S *own = slot(q - 1, 0);
+                const bool sa = cz(q) == -1 && topw, sb = cz(q) == 1 && botw;
+                const S *pa = sa ? own + I : b + (src + ca);
+                const S *pb = sb ? own + (I + 1u) : b + (src + 1u + cb);
+                v = SP::make(*pa, *pb);
             }
             hv[q - 1] = v;
         }
@@ -409,7 +424,13 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
             const float2 r = make_float2(cen.x, cen.z);
 
             // ---- decode with the sources' rest populations: g = h + 3 a
-            const float *fa[3] = {f0_plane(x - 1), f0_plane(x), f0_plane(x + 1)};
+            const float *fa[3];
+            {
+                const int s0 = fslot(x - 1), s1 = s0 + 1 == NF ? 0 : s0 + 1, s2 = s1 + 1 == NF ? 0 : s1 + 1;
+                fa[0] = sf0 + s0 * (AY * AZ);
+                fa[1] = sf0 + s1 * (AY * AZ);
+                fa[2] = sf0 + s2 * (AY * AZ);
+            }
             auto col = [&](int ccx, int ccy, int dzo) -> float2 {
                 return *reinterpret_cast<const float2 *>(fa[1 - ccx] + ac - ccy * AZ + dzo);
             };
@@ -471,11 +492,11 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
                         *reinterpret_cast<T *>(b + dst) = v;
                     } else {
                         // node A's destination across the bottom periodic edge, node B's across the top;
-                        // the solid node of a wall pair (A of (2, 3), B of (dz-4, dz-3)) stores
-                        // nothing here: its z neighbour is the pair's fluid node
+                        // the solid node of a wall pair (A of (2, 3), B of (dz-4, dz-3)) writes into
+                        // its own slot instead: its z neighbour is the pair's fluid node
                         const unsigned ca = (edge && cz(q) == -1) ? zsA : 0u, cb = (edge && cz(q) == 1) ? zsB : 0u;
-                        if (!botw) b[dst + ca] = SP::lo(v);
-                        if (!topw) b[dst + 1u + cb] = SP::hi(v);
+                        b[botw ? I : dst + ca] = SP::lo(v);
+                        b[topw ? I + 1u : dst + 1u + cb] = SP::hi(v);
                         // half-way bounce-back: a destination on a wall layer returns to the node's own slot
                         if ((cz(q) == 1 && topw) || (cz(q) == -1 && botw))
                             *reinterpret_cast<T *>(slot(opp(q) - 1, I)) = v;

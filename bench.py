@@ -251,7 +251,7 @@ def run_ours(args) -> None:
     alg = bytes_per.get(dom_name, bytes_per["step"])
     achieved = alg * units_per_launch / per_launch_s / 1e9
     peaks = measured_peaks()
-    traffic = None
+    traffic, traffic_source = None, None
     tp = os.path.join(ROOT, "profiles", f"{dom_name}_traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
@@ -259,10 +259,11 @@ def run_ours(args) -> None:
         key = f"{args.workload}_{args.storage}"
         if key in tj:
             traffic = tj[key]
+            traffic_source = ("not measured in this run: " + tj.get("_note", "ncu capture")).strip()
     roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / peaks["hbm_gbs"], 4),
-                "peak_source": peaks["source"], "traffic": traffic,
+                "peak_source": peaks["source"], "traffic": traffic, "traffic_source": traffic_source,
                 "alg_bytes_per_lu": alg,
                 "kernels_ms_per_step": {k: round(v[1] / max(1, v[0]) * (v[0] / args.steps), 4)
                                         for k, v in kt.items()}}
