@@ -172,7 +172,7 @@ __device__ __forceinline__ void issue_plane(const KParams<float> &p, const float
     }
 }
 
-template <class S, int TY, int TZ, int L, class SL>
+template <class S, int TY, int TZ, int L, bool REF, class SL>
 __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const SL &slots,
                                           const float *__restrict__ f0c, float *__restrict__ f0n,
                                           const float *__restrict__ rho, const int z0, const int y0, const int x0,
@@ -346,14 +346,12 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
                 v = *reinterpret_cast<const T *>(b + src);
             } else {
                 const unsigned ca = (edge && cz(q) == 1) ? zsA : 0u, cb = (edge && cz(q) == -1) ? zsB : 0u;
+                v = SP::make(b[src + ca], b[src + 1u + cb]);
                 // a source on a wall layer: the node's own slot (half-way
                 // bounce-back) -- node B of (2, 3) for cz = +1, node A of
-                // (dz-4, dz-3) for cz = -1; selected addresses, no branch
-                const S *own = slot(q - 1, 0);
-                const bool sa = cz(q) == -1 && topw, sb = cz(q) == 1 && botw;
-                const S *pa = sa ? own + I : b + (src + ca);
-                const S *pb = sb ? own + (I + 1u) : b + (src + 1u + cb);
-                v = SP::make(*pa, *pb);
+                // (dz-4, dz-3) for cz = -1 (the other node of each is solid)
+                if (cz(q) == 1 && botw) v = *reinterpret_cast<const T *>(slot(q - 1, I));
+                if (cz(q) == -1 && topw) v = *reinterpret_cast<const T *>(slot(q - 1, I));
             }
             hv[q - 1] = v;
         }
@@ -459,10 +457,10 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
                 float2 qp[Q];
 #pragma unroll
                 for (int a = 0; a < Q; ++a) qp[a] = make_float2(qa[a], qb[a]);
-                collide36<O>(g, r, make_float2(FA[0], FB[0]), make_float2(FA[1], FB[1]), make_float2(FA[2], FB[2]),
+                collide36<O, REF>(g, r, make_float2(FA[0], FB[0]), make_float2(FA[1], FB[1]), make_float2(FA[2], FB[2]),
                              p.ts, p.omts, qp, v2);
             } else {
-                collide36<O>(g, r, make_float2(FA[0], FB[0]), make_float2(FA[1], FB[1]), make_float2(FA[2], FB[2]),
+                collide36<O, REF>(g, r, make_float2(FA[0], FB[0]), make_float2(FA[1], FB[1]), make_float2(FA[2], FB[2]),
                              p.ts, p.omts, nullptr, v2);
             }
             if (fluA) mv2 = fmaxf(mv2, v2.x);
@@ -492,11 +490,11 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
                         *reinterpret_cast<T *>(b + dst) = v;
                     } else {
                         // node A's destination across the bottom periodic edge, node B's across the top;
-                        // the solid node of a wall pair (A of (2, 3), B of (dz-4, dz-3)) writes into
-                        // its own slot instead: its z neighbour is the pair's fluid node
+                        // the solid node of a wall pair (A of (2, 3), B of (dz-4, dz-3)) stores
+                        // nothing here: its z neighbour is the pair's fluid node
                         const unsigned ca = (edge && cz(q) == -1) ? zsA : 0u, cb = (edge && cz(q) == 1) ? zsB : 0u;
-                        b[botw ? I : dst + ca] = SP::lo(v);
-                        b[topw ? I + 1u : dst + 1u + cb] = SP::hi(v);
+                        if (!botw) b[dst + ca] = SP::lo(v);
+                        if (!topw) b[dst + 1u + cb] = SP::hi(v);
                         // half-way bounce-back: a destination on a wall layer returns to the node's own slot
                         if ((cz(q) == 1 && topw) || (cz(q) == -1 && botw))
                             *reinterpret_cast<T *>(slot(opp(q) - 1, I)) = v;
@@ -528,13 +526,14 @@ constexpr int pair_min_blocks()
     return NT >= 512 ? 1 : 512 / NT;
 }
 
-template <class S, int TY, int TZ, int L>
+// REF: the MRT rates follow the reference's pattern (collide36)
+template <class S, int TY, int TZ, int L, bool REF>
 __global__ void __launch_bounds__(TY *TZ / 2, pair_min_blocks<TY * TZ / 2>())
     k_pair_collide(KParams<float> p, int P, SlotTable<S> slots, const float *__restrict__ f0c,
                    float *__restrict__ f0n, const float *__restrict__ rho, int xl)
 {
     extern __shared__ __align__(128) float4 smem4[];
-    pair_tile<S, TY, TZ, L>(p, P, slots, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
+    pair_tile<S, TY, TZ, L, REF>(p, P, slots, f0c, f0n, rho, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl,
                             smem4);
 }
 

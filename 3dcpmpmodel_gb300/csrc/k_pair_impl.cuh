@@ -12,6 +12,19 @@ namespace pair_detail {
 template <int TY, int TZ, int L>
 constexpr size_t smem_bytes() { return PairRings<TY, TZ, L>::BYTES; }
 
+// The rates follow the reference's pattern: 1 except one value for moments
+// 2, 4, 6, 8 and one for 9, 11, 13, 14, 15 (FluidCuda.cu:154-157).
+inline bool reference_rates(const KParams<float> &p)
+{
+    for (int a : {0, 1, 3, 5, 7, 10, 12, 16, 17, 18})
+        if (p.ts[a] != 1.0f) return false;
+    for (int a : {4, 6, 8})
+        if (p.ts[a] != p.ts[2] || p.omts[a] != p.omts[2]) return false;
+    for (int a : {11, 13, 14, 15})
+        if (p.ts[a] != p.ts[9] || p.omts[a] != p.omts[9]) return false;
+    return true;
+}
+
 template <class S, int TY, int TZ, int L>
 void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, float *f0n, const float *rho,
               cudaStream_t st)
@@ -19,8 +32,11 @@ void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, fl
     const dim3 grid((p.dz + TZ - 1) / TZ, (p.dy + TY - 1) / TY, (p.dx + xl - 1) / xl);
     SlotTable<S> slots;
     for (int k = 0; k < Q - 1; ++k) slots.q[k] = h + (size_t)p.n * k;
-    k_pair_collide<S, TY, TZ, L><<<grid, TY * TZ / 2, smem_bytes<TY, TZ, L>(), st>>>(p, P, slots, f0c, f0n, rho,
-                                                                                    xl);
+    constexpr size_t sm = smem_bytes<TY, TZ, L>();
+    if (reference_rates(p))
+        k_pair_collide<S, TY, TZ, L, true><<<grid, TY * TZ / 2, sm, st>>>(p, P, slots, f0c, f0n, rho, xl);
+    else
+        k_pair_collide<S, TY, TZ, L, false><<<grid, TY * TZ / 2, sm, st>>>(p, P, slots, f0c, f0n, rho, xl);
 }
 
 template <class S, int TY, int TZ, int L>
@@ -28,8 +44,11 @@ bool set_attr_t(int max_smem)
 {
     const size_t b = smem_bytes<TY, TZ, L>();
     if ((int)b > max_smem) return false;
-    const bool ok = cudaFuncSetAttribute(k_pair_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)b) == cudaSuccess;
+    const bool ok =
+        cudaFuncSetAttribute(k_pair_collide<S, TY, TZ, L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)b) == cudaSuccess &&
+        cudaFuncSetAttribute(k_pair_collide<S, TY, TZ, L, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)b) == cudaSuccess;
     cudaGetLastError();
     return ok;
 }

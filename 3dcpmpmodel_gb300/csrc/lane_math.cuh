@@ -355,7 +355,15 @@ __device__ __forceinline__ void inverse36(const typename O::V m[Q], typename O::
 // qp36 = 36 x the K1/K2 pressure-tensor moments (FluidCuda.cu:260-266) or null;
 // out g = post-collision populations (same form), mv2 = |u + F / (2 rho)|^2 of
 // the colliding state, u = (jx, jy, jz) / rho from the moments of g.
-template <class O>
+//
+// REF: the rates follow the reference's pattern (FluidCuda.cu:154-157, what
+// ts_from_tau builds): s = 1 for moments 0, 1, 3, 5, 7, 10, 12, 16, 17, 18, one
+// rate for 2, 4, 6, 8 and one for 9, 11, 13, 14, 15.  A unit rate makes the
+// relaxed moment its forced equilibrium (1 - s = 0), so those moments need no
+// relaxation and 16-18 vanish; the compiler then drops what only they used.
+// The results are those of the general form (the zero terms it adds can only
+// change the sign of a zero).
+template <class O, bool REF = false>
 __device__ __forceinline__ void collide36(typename O::V g[Q], typename O::V rho, typename O::V Fx,
                                           typename O::V Fy, typename O::V Fz, const float ts[Q],
                                           const float omts[Q], const typename O::V *qp36, typename O::V &mv2)
@@ -377,7 +385,16 @@ __device__ __forceinline__ void collide36(typename O::V g[Q], typename O::V rho,
     meq36<O>(r36, O::fma(Fx, ir, ux), O::fma(Fy, ir, uy), O::fma(Fz, ir, uz), me1);
 #pragma unroll
     for (int a = 0; a < Q; ++a) {
-        V v = a >= 16 ? O::mul(O::k(omts[a]), m[a]) : O::fma(O::k(omts[a]), O::sub(m[a], me[a]), me1[a]);
+        V v;
+        if (!REF) {
+            v = a >= 16 ? O::mul(O::k(omts[a]), m[a]) : O::fma(O::k(omts[a]), O::sub(m[a], me[a]), me1[a]);
+        } else if (a == 2 || a == 4 || a == 6 || a == 8) {
+            v = O::fma(O::k(omts[2]), O::sub(m[a], me[a]), me1[a]);
+        } else if (a == 9 || a == 11 || a == 13 || a == 14 || a == 15) {
+            v = O::fma(O::k(omts[9]), O::sub(m[a], me[a]), me1[a]);
+        } else {
+            v = a >= 16 ? O::k(0.f) : me1[a];
+        }
         if (qp36) v = O::fma(qp36[a], O::k(ts[a]), v);
         m[a] = v;
     }

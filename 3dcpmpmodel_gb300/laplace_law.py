@@ -12,9 +12,12 @@ the device reductions give the Laplace probe of SaveDataOriDen
 pressure jump dp from the EOS at the inside and outside probes) and the FP64
 mass, before and after.  Laplace's law dp = 2 sigma / R is checked by a
 least-squares line dp = s (1/R) + c through the radii of each form: the
-surface tension is s / 2, and c should be near zero.  A droplet below the
-size that is stable in this closed box evaporates; its run has no crossing
-(R = 0) and is left out of the fit.  Prints one JSON line.
+surface tension is s / 2, and c should be near zero.  In this closed box a
+droplet started below a radius of about 21 evaporates into the vapour (the
+box's mean density then lies in the metastable vapour range); a run whose
+droplet is gone has no crossing (R = 0) and is left out of the fit, and the
+surviving droplets settle at a smaller radius than they started with.  Prints
+one JSON line with the probe densities of each run.
 """
 import argparse
 import importlib
@@ -34,8 +37,10 @@ def run(cp, scheme, storage, radius, steps):
     s.step(steps - 1)
     d = s.reduce()
     dt = time.perf_counter() - t
+    rho = s.get("rho").reshape(64, 64, 64)
     s.close()
     return dict(radius_init=radius, lap_r=d["lap_r"], lap_dp=d["lap_dp"], lap_sigma=d["lap_sigma"],
+                rho_in=float(rho[32, 32, 32]), rho_out=float(rho[32, 0, 32]),
                 mass_drift=(d["mass"] - m0) / m0, seconds=round(dt, 2))
 
 
@@ -54,7 +59,7 @@ def fit(rows):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=5000)
-    ap.add_argument("--radii", default="12,14,16,18,20")
+    ap.add_argument("--radii", default="21,22,23,24,25,26")
     args = ap.parse_args()
     cp = importlib.import_module("3dcpmpmodel_gb300")
     radii = [float(r) for r in args.radii.split(",")]
