@@ -3,7 +3,7 @@
     python -m 3dcpmpmodel_gb300.laplace_law [--steps 5000] [--radii 12,16,20]
 
 64^3 fully periodic box, CP-CS with a = 0.5, b = 4 at T/Tc = 0.85, kappa =
-0.01, tau = 1 (K = 0.2, the reference's default), a spherical droplet of each
+0.01, tau = 1, EOS scale K = 1 (K_EOS below), a spherical droplet of each
 radius centred in the box with the tanh width parameter 2 and the coexistence
 densities of the CS curve.  Each radius runs `--steps` steps in three forms:
 FUSED with FP16 storage, FUSED with FP32 storage and PLAIN FP64.  For each run
@@ -12,12 +12,10 @@ the device reductions give the Laplace probe of SaveDataOriDen
 pressure jump dp from the EOS at the inside and outside probes) and the FP64
 mass, before and after.  Laplace's law dp = 2 sigma / R is checked by a
 least-squares line dp = s (1/R) + c through the radii of each form: the
-surface tension is s / 2, and c should be near zero.  In this closed box a
-droplet started below a radius of about 21 evaporates into the vapour (the
-box's mean density then lies in the metastable vapour range); a run whose
-droplet is gone has no crossing (R = 0) and is left out of the fit, and the
-surviving droplets settle at a smaller radius than they started with.  Prints
-one JSON line with the probe densities of each run.
+surface tension is s / 2, and c should be near zero.  A droplet gives part
+of its mass to the vapour and settles at a smaller radius than it started
+with; a run whose droplet evaporated has no crossing (R = 0) and is left out
+of the fit.  Prints one JSON line with the probe densities of each run.
 """
 import argparse
 import importlib
@@ -27,8 +25,16 @@ import time
 import numpy as np
 
 
+# The EOS scale K of mu = K^2 mu0 - kappa lap(rho): 1, the unscaled
+# Carnahan-Starling form.  With the reference's default 0.2 the surface term
+# dominates in this closed 64^3 box: droplets of these sizes shrink or
+# evaporate for thousands of steps and the vapour stays far from coexistence,
+# so the probe does not measure an equilibrium pressure jump.
+K_EOS = 1.0
+
+
 def run(cp, scheme, storage, radius, steps):
-    s = cp.Solver(dx=64, dy=64, dz=64, model=206, tr=0.85, eos_a=0.5, eos_b=4.0, ka=0.01, tau=1.0,
+    s = cp.Solver(dx=64, dy=64, dz=64, model=206, tr=0.85, eos_a=0.5, eos_b=4.0, ka=0.01, tau=1.0, k=K_EOS,
                   wall_mode=0, scheme=cp.SCHEME[scheme], storage=cp.STORE[storage])
     s.set_flow_field(radius=radius, width=2.0, centre=(32.0, 32.0, 32.0))
     s.step(1)
@@ -59,11 +65,12 @@ def fit(rows):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=5000)
-    ap.add_argument("--radii", default="21,22,23,24,25,26")
+    ap.add_argument("--radii", default="10,12,14,16,18,20")
     args = ap.parse_args()
     cp = importlib.import_module("3dcpmpmodel_gb300")
     radii = [float(r) for r in args.radii.split(",")]
-    out = {"box": "64^3 periodic", "eos": "CS a=0.5 b=4", "tr": 0.85, "steps": args.steps, "forms": {}}
+    out = {"box": "64^3 periodic", "eos": "CS a=0.5 b=4", "tr": 0.85, "K": K_EOS, "steps": args.steps,
+           "forms": {}}
     for scheme, storage in (("plain", "f64"), ("fused", "f32"), ("fused", "f16")):
         rows = [run(cp, scheme, storage, r, args.steps) for r in radii]
         out["forms"][f"{scheme}_{storage}"] = {"runs": rows, "fit": fit(rows)}
