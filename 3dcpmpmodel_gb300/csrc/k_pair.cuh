@@ -248,16 +248,14 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
     int roff[RG::KM], moff[RG::KM], wcol[RG::KM], wflag[RG::KM];
 #pragma unroll
     for (int k = 0; k < RG::KM; ++k) {
-        // the last round's surplus threads repeat the plane's last element
-        // (same value, same slot): every thread runs every round unbranched
-        const int e = min(tid + k * NT, RG::NPM - 1);
+        const int e = tid + k * NT;
         const int r = e / HM, c = e - (e / HM) * HM;
         roff[k] = (r + L) * RZ + 4 + 2 * c;
         moff[k] = r * MZ + 2 * c;
         const int z = z0 - 4 + 2 * c;
         // bit 0 / 1: element z / z + 1 is solid; bit 2: the top wall
         const int sa = walled && (z < 3 || z > p.dz - 4), sb = walled && (z + 1 < 3 || z + 1 > p.dz - 4);
-        wflag[k] = sa | (sb << 1) | ((z > p.dz / 2) << 2);
+        wflag[k] = (e < RG::NPM) ? (sa | (sb << 1) | ((z > p.dz / 2) << 2)) : 0;
         wcol[k] = wrap_small(y0 - 3 + r, p.dy);
     }
     auto comp_mu = [&](int pl) {
@@ -279,6 +277,7 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
         auto ld = [](const float *b, int i) { return *reinterpret_cast<const float2 *>(b + i); };
 #pragma unroll
         for (int k = 0; k < RG::KM; ++k) {
+            if (k * NT + tid >= RG::NPM) break;
             const int c = roff[k];
             const float2 r0 = ld(rc, c);
             const float2 lo = ld(rc, c - 2), hi = ld(rc, c + 2);

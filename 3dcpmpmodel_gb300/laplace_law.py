@@ -14,8 +14,9 @@ mass, before and after.  Laplace's law dp = 2 sigma / R is checked by a
 least-squares line dp = s (1/R) + c through the radii of each form: the
 surface tension is s / 2, and c should be near zero.  A droplet gives part
 of its mass to the vapour and settles at a smaller radius than it started
-with; a run whose droplet evaporated has no crossing (R = 0) and is left out
-of the fit.  Prints one JSON line with the probe densities of each run.
+with; a droplet started too small evaporates, and its run is left out of the
+fit (the probe's inside and outside densities no longer differ).  Prints one
+JSON line with the probe densities of each run.
 """
 import argparse
 import importlib
@@ -50,8 +51,15 @@ def run(cp, scheme, storage, radius, steps):
                 mass_drift=(d["mass"] - m0) / m0, seconds=round(dt, 2))
 
 
-def fit(rows):
-    rows = [r for r in rows if r["lap_r"] > 0]  # a droplet that evaporated has no crossing
+def droplet(r, gap):
+    """The probe sees a droplet: inside and outside densities differ by more
+    than half the coexistence gap (an evaporated droplet leaves a uniform
+    vapour, where the crossing search can still find a noise crossing)."""
+    return r["lap_r"] > 0 and r["rho_in"] - r["rho_out"] > 0.5 * gap
+
+
+def fit(rows, gap):
+    rows = [r for r in rows if droplet(r, gap)]
     if len(rows) < 2:
         return None
     inv_r = np.array([1.0 / r["lap_r"] for r in rows])
@@ -59,7 +67,9 @@ def fit(rows):
     A = np.vstack([inv_r, np.ones_like(inv_r)]).T
     (slope, icpt), *_ = np.linalg.lstsq(A, dp, rcond=None)
     resid = dp - A @ np.array([slope, icpt])
-    return dict(sigma=slope / 2, intercept=icpt, max_resid_rel=float(np.max(np.abs(resid)) / np.max(np.abs(dp))))
+    sig = [r["lap_dp"] * r["lap_r"] / 2 for r in rows]
+    return dict(sigma=slope / 2, intercept=icpt, max_resid_rel=float(np.max(np.abs(resid)) / np.max(np.abs(dp))),
+                sigma_per_run=sig, droplets=len(rows))
 
 
 def main():
@@ -68,15 +78,17 @@ def main():
     ap.add_argument("--radii", default="10,12,14,16,18,20")
     args = ap.parse_args()
     cp = importlib.import_module("3dcpmpmodel_gb300")
+    co = cp.coexistence(206, 0.85, 0.5, 4.0)
+    gap = co["den_l"] - co["den_g"]
     radii = [float(r) for r in args.radii.split(",")]
     out = {"box": "64^3 periodic", "eos": "CS a=0.5 b=4", "tr": 0.85, "K": K_EOS, "steps": args.steps,
            "forms": {}}
     for scheme, storage in (("plain", "f64"), ("fused", "f32"), ("fused", "f16")):
         rows = [run(cp, scheme, storage, r, args.steps) for r in radii]
-        out["forms"][f"{scheme}_{storage}"] = {"runs": rows, "fit": fit(rows)}
+        out["forms"][f"{scheme}_{storage}"] = {"runs": rows, "fit": fit(rows, gap)}
     ref = out["forms"]["plain_f64"]["runs"]
     for k, v in out["forms"].items():
-        both = [(a, b) for a, b in zip(v["runs"], ref) if a["lap_r"] > 0 and b["lap_r"] > 0]
+        both = [(a, b) for a, b in zip(v["runs"], ref) if droplet(a, gap) and droplet(b, gap)]
         v["max_dp_rel_vs_f64"] = max((abs(a["lap_dp"] - b["lap_dp"]) / abs(b["lap_dp"]) for a, b in both), default=None)
         v["max_r_abs_vs_f64"] = max((abs(a["lap_r"] - b["lap_r"]) for a, b in both), default=None)
     print(json.dumps(out))
