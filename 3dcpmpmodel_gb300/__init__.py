@@ -230,16 +230,22 @@ class Solver:
         t["collide_ms"] = ms.value
         return t
 
-    def set_tile(self, tile_y: int, tile_z: int, march_x: int, nodes_per_thread: int = 1):
+    def set_tile(self, tile_y: int, tile_z: int, march_x: int, nodes_per_thread: int = 1, form: int = 0):
         """Column tile (tile_y x tile_z nodes), x-march length and nodes per
-        thread (1, or 2 for the paired kernel) of the fused collide."""
-        _abi.check(self._lib.cpmp_set_tile_ex(self._h, int(tile_y), int(tile_z), int(march_x),
-                                              int(nodes_per_thread)))
+        thread (1, or 2 for the paired kernel) of the fused collide; form 0
+        runs it in one pass, 1 as a force pass (the tile is its) and a
+        collide-stream pass (node pairs)."""
+        _abi.check(self._lib.cpmp_set_tile_form(self._h, int(tile_y), int(tile_z), int(march_x),
+                                                int(nodes_per_thread), int(form)))
 
     def tile(self) -> dict:
         v = [C.c_int() for _ in range(4)]
         _abi.check(self._lib.cpmp_get_tile(self._h, *(C.byref(x) for x in v)))
-        return dict(zip(("tile_y", "tile_z", "march_x", "nodes_per_thread"), (x.value for x in v)))
+        t = dict(zip(("tile_y", "tile_z", "march_x", "nodes_per_thread"), (x.value for x in v)))
+        f = C.c_int()
+        _abi.check(self._lib.cpmp_get_form(self._h, C.byref(f)))
+        t["form"] = f.value
+        return t
 
     # timing ------------------------------------------------------------------------
     @property

@@ -87,6 +87,8 @@ SIGNATURES = {
     "cpmp_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "cpmp_set_tile_ex": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "cpmp_get_tile": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 4),
+    "cpmp_set_tile_form": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "cpmp_get_form": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "cpmp_stream": (C.c_void_p, [C.c_void_p]),
     "cpmp_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "cpmp_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),

@@ -32,6 +32,10 @@ UNITS = [
     ("k_pair_f16.cu", ["--fmad=false"]),
     ("k_pair_bf16.cu", ["--fmad=false"]),
     ("k_pair_f32.cu", ["--fmad=false"]),
+    ("k_split_force.cu", ["--fmad=false"]),
+    ("k_split_f16.cu", ["--fmad=false"]),
+    ("k_split_bf16.cu", ["--fmad=false"]),
+    ("k_split_f32.cu", ["--fmad=false"]),
     ("k_diag.cu", []),
     ("k_adjoint_f32.cu", []),
     ("k_adjoint_f64.cu", ["--fmad=false"]),

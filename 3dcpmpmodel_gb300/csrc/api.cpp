@@ -157,6 +157,19 @@ cpmp_status dalloc(void **ptr, size_t bytes, const char *what)
     return CPMP_OK;
 }
 
+// The two-pass form's force field (FUSED scheme; the PLAIN scheme's F is its
+// own field), allocated when that form is first selected: 3 floats per node,
+// 6 with the K1/K2 term (grad rho).
+size_t force_field_bytes(const cpmp_handle *h)
+{
+    return ((h->p.k1 != 0.0 || h->p.k2 != 0.0) ? 6 : 3) * (size_t)h->n * sizeof(float);
+}
+cpmp_status ensure_force_field(cpmp_handle *h)
+{
+    if (h->plain || h->F) return CPMP_OK;
+    return dalloc(&h->F, force_field_bytes(h), "F");
+}
+
 // Heuristic default tile for the fused kernel (the autotuner refines it):
 // the paired kernel where the grid allows it.
 FusedTile default_tile(const cpmp_params &p)
@@ -192,6 +205,12 @@ cpmp_status upload_wall(cpmp_handle *h, const std::vector<double> &w)
     return CPMP_OK;
 }
 
+// kernel launches of one time step (the two-pass form adds its force pass)
+long long step_launches(const cpmp_handle *h)
+{
+    return h->launches_per_step + ((!h->plain && h->tile.form == 1) ? 1 : 0);
+}
+
 // one time step, launched directly (no graph)
 void launch_one_step(cpmp_handle *h, LaunchHook *hook)
 {
@@ -214,12 +233,13 @@ void launch_one_step(cpmp_handle *h, LaunchHook *hook)
         if (h->sdiag) cudaMemsetAsync(h->sdiag + P * h->sdiag_stride, 0, sizeof(unsigned), h->st);
         fused_launch_wall(k, (float *)h->rho, (float *)h->rho2, h->st, hook);
         fused_launch_collide(h->p.storage, k, P, h->tile, h->h, h->f0[P], h->f0[1 - P], (const float *)h->rho,
+                             (float *)h->F,
                              h->st, hook);
         fused_launch_density(h->p.storage, k, 1 - P, h->h, h->f0[1 - P], (float *)h->rho2, h->st, hook);
         std::swap(h->rho, h->rho2);
     }
     h->step += 1;
-    h->launches += h->launches_per_step;
+    h->launches += step_launches(h);
 }
 
 bool step_parity_even(const cpmp_handle *h) { return h->plain ? h->cur == 0 : (h->step & 1) == 0; }
@@ -574,7 +594,7 @@ cpmp_status cpmp_step(cpmp_handle *h, int nsteps)
         while (left >= 2) {
             CK(cudaGraphLaunch(h->gexec, h->st));
             h->step += 2;
-            h->launches += 2LL * h->launches_per_step;
+            h->launches += 2LL * step_launches(h);
             left -= 2;  // two lattice swaps leave h->cur unchanged
         }
     }
@@ -841,12 +861,12 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     const size_t n = (size_t)h->n;
     const size_t hs = h->p.storage == CPMP_STORE_F32 ? 4 : 2;
     // scratch copy of the state: the in-place A-A kernel would otherwise advance it
-    void *sh = nullptr, *sf0a = nullptr, *sf0b = nullptr, *srho = nullptr;
+    void *sh = nullptr, *sf0a = nullptr, *sf0b = nullptr, *srho = nullptr, *sF = nullptr;
     cpmp_status s;
     if ((s = dalloc(&sh, (CPMP_Q - 1) * n * hs, "tune h")) != CPMP_OK) return s;
     if ((s = dalloc(&sf0a, n * 4, "tune f0")) != CPMP_OK || (s = dalloc(&sf0b, n * 4, "tune f0")) != CPMP_OK ||
-        (s = dalloc(&srho, n * 4, "tune rho")) != CPMP_OK) {
-        cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho);
+        (s = dalloc(&srho, n * 4, "tune rho")) != CPMP_OK || (s = dalloc(&sF, force_field_bytes(h), "tune F")) != CPMP_OK) {
+        cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(sF);
         return s;
     }
     const int P0 = (int)(h->step & 1);
@@ -864,7 +884,7 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     for (int t = 0; t < fused_tile_count(); ++t) {
         for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
-            if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz, ft.np)) continue;
+            if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz, ft.np, ft.form)) continue;
             if (ft.np == 2 && !pair_grid_ok(h->p.dz)) continue;
             if (ft.xl > h->p.dx && xi > 0) continue;
             if (ft.ty > 2 * h->p.dy && ft.ty > 1) continue;
@@ -872,22 +892,22 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
             ft.xl = std::min(ft.xl, h->p.dx);
             // warm-up, then time two launches (one of each parity)
             fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
-                                 (const float *)srho, h->st, nullptr);
+                                 (const float *)srho, (float *)sF, h->st, nullptr);
             cudaEventRecord(e0, h->st);
             fused_launch_collide(h->p.storage, k, 1, ft, sh, (const float *)sf0b, (float *)sf0a,
-                                 (const float *)srho, h->st, nullptr);
+                                 (const float *)srho, (float *)sF, h->st, nullptr);
             fused_launch_collide(h->p.storage, k, 0, ft, sh, (const float *)sf0a, (float *)sf0b,
-                                 (const float *)srho, h->st, nullptr);
+                                 (const float *)srho, (float *)sF, h->st, nullptr);
             cudaEventRecord(e1, h->st);
             cudaError_t e = cudaEventSynchronize(e1);
             if (e != cudaSuccess) {
                 cudaEventDestroy(e0); cudaEventDestroy(e1);
-                cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho);
+                cudaFree(sh); cudaFree(sf0a); cudaFree(sf0b); cudaFree(srho); cudaFree(sF);
                 return fail(CPMP_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
             }
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
-            h->launches += 3;
+            h->launches += ft.form == 1 ? 6 : 3;
             if (ms / 2 < best_ms) {
                 best_ms = ms / 2;
                 best = ft;
@@ -900,8 +920,11 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     cudaFree(sf0a);
     cudaFree(sf0b);
     cudaFree(srho);
+    cudaFree(sF);
     CK(cudaGetLastError());
-    if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl || best.np != h->tile.np) {
+    if (best.form == 1 && (s = ensure_force_field(h)) != CPMP_OK) return s;
+    if (best.ty != h->tile.ty || best.tz != h->tile.tz || best.xl != h->tile.xl || best.np != h->tile.np ||
+        best.form != h->tile.form) {
         h->tile = best;
         if (h->gexec) {
             cudaGraphExecDestroy(h->gexec);
@@ -920,6 +943,19 @@ cpmp_status cpmp_set_tile(cpmp_handle *h, int tile_y, int tile_z, int march_x)
     return cpmp_set_tile_ex(h, tile_y, tile_z, march_x, 1);
 }
 
+cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread)
+{
+    return cpmp_set_tile_form(h, tile_y, tile_z, march_x, nodes_per_thread, CPMP_FORM_ONE_PASS);
+}
+
+cpmp_status cpmp_get_form(cpmp_handle *h, int *form)
+{
+    if (!h) return fail(CPMP_ERR_PARAM, "null handle");
+    if (h->plain) return fail(CPMP_ERR_UNSUPPORTED, "step forms apply to the FUSED scheme");
+    if (form) *form = h->tile.form;
+    return CPMP_OK;
+}
+
 cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread)
 {
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
@@ -931,17 +967,25 @@ cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     return CPMP_OK;
 }
 
-cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread)
+cpmp_status cpmp_set_tile_form(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread, int form)
 {
     if (!h) return fail(CPMP_ERR_PARAM, "null handle");
     if (h->plain) return fail(CPMP_ERR_UNSUPPORTED, "tiles apply to the FUSED scheme");
     if (march_x < 1) return fail(CPMP_ERR_PARAM, "march_x must be >= 1");
     if (nodes_per_thread != 1 && nodes_per_thread != 2) return fail(CPMP_ERR_PARAM, "nodes_per_thread must be 1 or 2");
-    if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z, nodes_per_thread))
+    if (form != CPMP_FORM_ONE_PASS && form != CPMP_FORM_TWO_PASS) return fail(CPMP_ERR_PARAM, "unknown step form");
+    if (form == CPMP_FORM_TWO_PASS && nodes_per_thread != 2)
+        return fail(CPMP_ERR_PARAM, "the two-pass form runs node pairs (nodes_per_thread 2)");
+    if (!fused_tile_usable(h->p.storage, h->p.lap_order, tile_y, tile_z, nodes_per_thread, form))
         return fail(CPMP_ERR_UNSUPPORTED, "tile not instantiated or too large for this device");
     if (nodes_per_thread == 2 && !pair_grid_ok(h->p.dz))
-        return fail(CPMP_ERR_UNSUPPORTED, "the paired kernel needs DZ a multiple of 4");
-    h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx), nodes_per_thread};
+        return fail(CPMP_ERR_UNSUPPORTED, "the paired kernels need DZ a multiple of 4");
+    CK(cudaSetDevice(h->p.device));
+    if (form == CPMP_FORM_TWO_PASS) {
+        const cpmp_status s = ensure_force_field(h);
+        if (s != CPMP_OK) return s;
+    }
+    h->tile = FusedTile{tile_y, tile_z, std::min(march_x, h->p.dx), nodes_per_thread, form};
     if (h->gexec) {
         cudaGraphExecDestroy(h->gexec);
         h->gexec = nullptr;

@@ -110,9 +110,11 @@ __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, con
 
 // ------------------------------------------------------------- dispatch ----
 namespace {
-// (ty, tz, nodes per thread)
-constexpr int kTiles[][3] = {{4, 32, 1}, {8, 32, 1}, {16, 32, 1}, {16, 16, 1}, {8, 16, 1},
-                             {8, 32, 2}, {16, 32, 2}, {8, 64, 2}, {4, 64, 2}, {16, 64, 2}};
+// (ty, tz, nodes per thread, form): form 1 is the two-pass step, whose
+// column tile is the force pass's
+constexpr int kTiles[][4] = {{4, 32, 1, 0},  {8, 32, 1, 0},  {16, 32, 1, 0}, {16, 16, 1, 0}, {8, 16, 1, 0},
+                             {8, 32, 2, 0},  {16, 32, 2, 0}, {8, 64, 2, 0},  {4, 64, 2, 0},  {16, 64, 2, 0},
+                             {8, 32, 2, 1},  {16, 32, 2, 1}, {8, 64, 2, 1},  {4, 64, 2, 1},  {16, 64, 2, 1}};
 constexpr int kNumTiles = sizeof(kTiles) / sizeof(kTiles[0]);
 
 template <class F>
@@ -159,10 +161,10 @@ bool pair_set_attr(int storage, int lap_order, int ty, int tz, int max_smem)
 // memory fits the device's opt-in limit
 bool g_usable[3][2][kNumTiles];
 int storage_index(int storage) { return storage == CPMP_STORE_F16 ? 0 : (storage == CPMP_STORE_BF16 ? 1 : 2); }
-int tile_index(int ty, int tz, int np = 1)
+int tile_index(int ty, int tz, int np = 1, int form = 0)
 {
     for (int i = 0; i < kNumTiles; ++i)
-        if (kTiles[i][0] == ty && kTiles[i][1] == tz && kTiles[i][2] == np) return i;
+        if (kTiles[i][0] == ty && kTiles[i][1] == tz && kTiles[i][2] == np && kTiles[i][3] == form) return i;
     return -1;
 }
 
@@ -190,14 +192,17 @@ void set_attr_l(int si, int max_smem)
 }
 }  // namespace
 
-bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np)
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np, int form)
 {
-    const int t = tile_index(ty, tz, np);
+    const int t = tile_index(ty, tz, np, form);
     return t >= 0 && g_usable[storage_index(storage)][lap_order == 7 ? 1 : 0][t];
 }
 
 int fused_tile_count() { return kNumTiles; }
-FusedTile fused_tile(int idx, int xl) { return FusedTile{kTiles[idx][0], kTiles[idx][1], xl, kTiles[idx][2]}; }
+FusedTile fused_tile(int idx, int xl)
+{
+    return FusedTile{kTiles[idx][0], kTiles[idx][1], xl, kTiles[idx][2], kTiles[idx][3]};
+}
 
 cudaError_t fused_setup_attributes()
 {
@@ -216,7 +221,9 @@ cudaError_t fused_setup_attributes()
         if (kTiles[i][2] != 2) continue;
         for (int si = 0; si < 3; ++si)
             for (int l = 0; l < 2; ++l)
-                g_usable[si][l][i] = pair_set_attr(storages[si], l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem);
+                g_usable[si][l][i] = kTiles[i][3] == 1
+                                         ? split_force_set_attr(l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem)
+                                         : pair_set_attr(storages[si], l ? 7 : 5, kTiles[i][0], kTiles[i][1], max_smem);
     }
     return cudaSuccess;
 }
@@ -245,9 +252,23 @@ void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, c
 }
 
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, cudaStream_t st,
+                          const float *f0c, float *f0n, const float *rho, float *F, cudaStream_t st,
                           LaunchHook *hook)
 {
+    if (t.form == 1) {
+        hook_begin(hook, K_FORCE, st);
+        split_force_launch(p, t, rho, F, st);
+        hook_end(hook, K_FORCE, st);
+        hook_begin(hook, K_FUSED, st);
+        if (storage == CPMP_STORE_F16)
+            split_collide_launch_f16(p, P, h, f0c, f0n, rho, F, st);
+        else if (storage == CPMP_STORE_BF16)
+            split_collide_launch_bf16(p, P, h, f0c, f0n, rho, F, st);
+        else
+            split_collide_launch_f32(p, P, h, f0c, f0n, rho, F, st);
+        hook_end(hook, K_FUSED, st);
+        return;
+    }
     hook_begin(hook, K_FUSED, st);
     if (t.np == 2 && storage == CPMP_STORE_F16)
         pair_launch_f16(p, P, t, h, f0c, f0n, rho, st);

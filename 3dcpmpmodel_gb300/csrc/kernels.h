@@ -52,13 +52,17 @@ extern template void plain_launch_mu_force<double>(const KParams<double> &, cons
 struct FusedTile {
     int ty, tz, xl;
     int np = 1;
+    // 0: one pass (mu, force, collision and streaming in one kernel);
+    // 1: two passes (k_split.cuh: force pass with this column tile, then the
+    //    shared-memory-free collide pass), np = 2
+    int form = 0;
 };
 // Tile shapes instantiated for the fused kernel; the autotuner picks among
 // them per grid.
 int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
 // The (storage, Laplacian, tile) instantiation fits this device's shared memory.
-bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1);
+bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1, int form = 0);
 // The paired kernel's grid requirement: DZ a multiple of 4.
 inline bool pair_grid_ok(int dz) { return dz % 4 == 0; }
 // Paired kernel (k_pair_<storage>.cu, one unit per storage type): each
@@ -71,6 +75,19 @@ CPMP_PAIR_DECL(f16)
 CPMP_PAIR_DECL(bf16)
 CPMP_PAIR_DECL(f32)
 #undef CPMP_PAIR_DECL
+// Two-pass form (k_split_force.cu, k_split_<storage>.cu).  The force pass
+// writes F[c * n + I] (c = 0..2; 3..5 grad(rho) with the K1/K2 term) with the
+// paired column tile (ty, tz) and march xl; false when (ty, tz) is not one of
+// its shapes.
+bool split_force_set_attr(int lap_order, int ty, int tz, int max_smem);
+bool split_force_launch(const KParams<float> &p, const FusedTile &t, const float *rho, float *F, cudaStream_t st);
+#define CPMP_SPLIT_DECL(SUFFIX)                                                                                  \
+    void split_collide_launch_##SUFFIX(const KParams<float> &p, int P, void *h, const float *f0c, float *f0n,   \
+                                       const float *rho, const float *F, cudaStream_t st);
+CPMP_SPLIT_DECL(f16)
+CPMP_SPLIT_DECL(bf16)
+CPMP_SPLIT_DECL(f32)
+#undef CPMP_SPLIT_DECL
 
 cudaError_t fused_setup_attributes();
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
@@ -79,8 +96,11 @@ void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d
 // rho_mirror when it is non-null (the other density buffer).
 void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, cudaStream_t st, LaunchHook *hook);
 // The fused collide reads rho, this step's density (wall layers included).
+// F: the two-pass form's force field (3 n floats, 6 n with the K1/K2 term;
+// unused by the one-pass form).
 void fused_launch_collide(int storage, const KParams<float> &p, int P, const FusedTile &t, void *h,
-                          const float *f0c, float *f0n, const float *rho, cudaStream_t st, LaunchHook *hook);
+                          const float *f0c, float *f0n, const float *rho, float *F, cudaStream_t st,
+                          LaunchHook *hook);
 // Density of the post-stream populations at parity P, every fluid node.
 void fused_launch_density(int storage, const KParams<float> &p, int P, const void *h,
                           const float *f0, float *rho, cudaStream_t st, LaunchHook *hook);

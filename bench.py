@@ -7,7 +7,7 @@ the 129 MB L2, so no L2 flush is needed between steps).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload c3|c2|c1|c4|c3ref] [--storage f16|bf16|f32] [--scheme fused|plain]
-                    [--tile ty,tz,xl[,np]] [--profile-case X,Y,Z]
+                    [--tile ty,tz,xl[,np[,form]]] [--profile-case X,Y,Z]
 
 Under torchrun (N > 1) every rank runs an independent replica (the step does
 not shard on one GPU per box); value is the sum over ranks, time the max.
@@ -66,18 +66,27 @@ def storage_bytes(storage: str) -> int:
     return {"f16": 2, "bf16": 2, "f32": 4, "f64": 8}[storage]
 
 
-def algorithmic_bytes(scheme: str, storage: str) -> dict:
+def algorithmic_bytes(scheme: str, storage: str, form: int = 0, kterm: bool = False) -> dict:
     """Algorithmic bytes per lattice update.
 
     B_LU = 2*19*s + 8 is the step-level unit (every population read and
     written once, one FP32 density written and read once).  Per kernel of the
     FUSED scheme: the fused collide reads and writes 18 moving populations of
     s bytes plus the FP32 rest population, and reads the density (4 B);
-    the density pass reads the populations and writes the density."""
+    the density pass reads the populations and writes the density.  In the
+    two-pass form (form 1) the force pass reads the density and writes the
+    FP32 force (12 B; 24 B with grad(rho) for the K1/K2 term), which the
+    collide pass reads back."""
     s = storage_bytes(storage)
     b_lu = 2 * Q * s + 8
     if scheme == "fused":
-        return {"step": b_lu, "fused_collide": 2 * (18 * s + 4) + 4, "density": 18 * s + 4 + 4}
+        collide = 2 * (18 * s + 4) + 4
+        d = {"step": b_lu, "fused_collide": collide, "density": 18 * s + 4 + 4}
+        if form == 1:
+            fb = 24 if kterm else 12
+            d["fused_collide"] = collide + fb
+            d["force"] = 4 + fb
+        return d
     r = 8 if storage == "f64" else 4
     return {"step": b_lu, "collide_stream": 2 * Q * r + 12 * r + 1, "macro": Q * r + 4 * r + 1}
 
@@ -243,7 +252,7 @@ def run_ours(args) -> None:
     s.sync()
     kt = s.kernel_times()
     s.kernel_timing(False)
-    bytes_per = algorithmic_bytes(args.scheme, args.storage)
+    bytes_per = algorithmic_bytes(args.scheme, args.storage, (tile or {}).get("form", 0))
     dom = max(kt.items(), key=lambda kv: kv[1][1])
     dom_name, (dom_launches, dom_ms) = dom
     per_launch_s = dom_ms / dom_launches / 1e3
@@ -256,7 +265,7 @@ def run_ours(args) -> None:
     if os.path.exists(tp):
         with open(tp) as f:
             tj = json.load(f)
-        key = f"{args.workload}_{args.storage}"
+        key = f"{args.workload}_{args.storage}" + ("_twopass" if (tile or {}).get("form", 0) == 1 else "")
         if key in tj:
             traffic = tj[key]
             traffic_source = ("not measured in this run: " + tj.get("_note", "ncu capture")).strip()
@@ -588,7 +597,9 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=2_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--tile", default="", help="ty,tz,xl[,np]: this fused tile instead of the autotuner's")
+    ap.add_argument("--tile", default="",
+                    help="ty,tz,xl[,np[,form]]: this fused tile (form 1: the two-pass step) instead of the "
+                         "autotuner's")
     ap.add_argument("--profile-case", default="",
                     help="X,Y,Z: only run --steps steps of a box of this grid with the workload's physics "
                          "(for profilers; no timing)")

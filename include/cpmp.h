@@ -228,6 +228,23 @@ cpmp_status cpmp_set_tile_ex(cpmp_handle *h, int tile_y, int tile_z, int march_x
 /* The tile in use (after cpmp_autotune: the one it kept).  Outputs may be NULL. */
 cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x, int *nodes_per_thread);
 
+/* Step forms of the FUSED scheme (no reference counterpart: the reference
+ * always runs ChemPotential, NonidealForce and GlobalCollide as separate
+ * kernels, FluidCuda.cu:1277-1292).  Both forms give the same results bit for
+ * bit.
+ *   CPMP_FORM_ONE_PASS  mu, the force, the collision and the A-A streaming of
+ *                       a node in one kernel (the column tile is that kernel's);
+ *   CPMP_FORM_TWO_PASS  a force pass (mu and F on a shared-memory column tile,
+ *                       written to an FP32 field of 12 bytes per node, 24 with
+ *                       the K1/K2 term) and a collide-stream pass without
+ *                       shared memory; node pairs (nodes_per_thread 2), DZ a
+ *                       multiple of 4, the column tile is the force pass's.
+ * cpmp_autotune times both forms; cpmp_set_tile_ex selects the one-pass form. */
+enum { CPMP_FORM_ONE_PASS = 0, CPMP_FORM_TWO_PASS = 1 };
+cpmp_status cpmp_set_tile_form(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread,
+                               int form);
+cpmp_status cpmp_get_form(cpmp_handle *h, int *form);
+
 /* The CUDA stream the handle launches on (cudaStream_t). */
 void *cpmp_stream(cpmp_handle *h);
 

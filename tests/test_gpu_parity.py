@@ -216,6 +216,46 @@ def test_paired_kernel_matches_single_node_kernel(cpmp, cfg, storage):
         assert np.array_equal(d, runs[0][1])
 
 
+@pytest.mark.parametrize("cfg", [
+    dict(dx=20, dy=18, dz=36, radius=7.0, width=4.0, base_pt=-0.04),                      # walls, partial z tile
+    dict(dx=24, dy=20, dz=32, radius=6.0, width=3.0, wall_mode=0, centre=(12, 10, 15)),   # periodic edges
+    dict(dx=20, dy=18, dz=28, radius=6.0, width=4.0, base_pt=0.02, K1=0.002, K2=-0.002, tau=1.0,
+         lap_order=7),                                                                    # K1/K2, 7-point
+    dict(dx=18, dy=12, dz=24, radius=5.0, width=3.0, model=205, tr=0.75),                  # RKS, walls
+], ids=["walls", "periodic", "k1k2_lap7", "rks"])
+@pytest.mark.parametrize("storage", ["f16", "bf16", "f32"])
+def test_two_pass_form_matches_one_pass(cpmp, cfg, storage):
+    """The two-pass form (force pass on a column tile, then the collide pass
+    without shared memory) gives exactly the bits of the one-pass kernels:
+    both parities, graph replay, walls, periodic x / y / z edges, partial
+    tiles, the K1/K2 term and the 7-point Laplacian."""
+    runs = []
+    for ty, tz, xl, form in ((8, 32, 9, 0), (8, 32, 9, 1), (16, 64, 11, 1), (4, 64, 7, 1), (16, 32, 5, 1)):
+        s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
+        s.set_tile(ty, tz, xl, 2, form)
+        assert s.tile()["form"] == form
+        s.step(11)
+        runs.append((s.get("rho"), s.get("dist"), s.reduce()["max_speed"]))
+        s.close()
+    assert np.isfinite(runs[0][0]).all() and np.isfinite(runs[0][1]).all()
+    for r, d, v in runs[1:]:
+        assert np.array_equal(r, runs[0][0])
+        assert np.array_equal(d, runs[0][1])
+        assert v == runs[0][2]
+
+
+def test_two_pass_form_needs_pairs_and_dz_multiple_of_four(cpmp):
+    s = solver_for(cpmp, dict(dx=20, dy=18, dz=37, radius=7.0, width=4.0), scheme="fused", storage="f16")
+    with pytest.raises(cpmp.CpmpError) as e:
+        s.set_tile(8, 32, 9, 2, 1)
+    assert e.value.status == 7
+    s.close()
+    s = solver_for(cpmp, dict(dx=20, dy=18, dz=36, radius=7.0, width=4.0), scheme="fused", storage="f16")
+    with pytest.raises(cpmp.CpmpError):
+        s.set_tile(8, 32, 9, 1, 1)
+    s.close()
+
+
 def test_paired_kernel_needs_dz_multiple_of_four(cpmp):
     s = solver_for(cpmp, dict(dx=20, dy=18, dz=37, radius=7.0, width=4.0), scheme="fused", storage="f16")
     with pytest.raises(cpmp.CpmpError) as e:
