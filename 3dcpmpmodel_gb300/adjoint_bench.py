@@ -40,13 +40,11 @@ def setup(storage, L=96, radius=24.0, scheme="plain"):
     return {"params": p, "droplet": dict(radius=radius, width=4.0, centre=(L / 2, L / 2, 3.0))}
 
 
-def main():
+def measure(steps: int = 2000, size: int = 96, fd: bool = False) -> dict:
+    """The adjoint-versus-forward record of the wall-field inversion set-up
+    (see the module docstring) as a dict."""
     import torch
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--size", type=int, default=96)
-    ap.add_argument("--fd", action="store_true")
-    a = ap.parse_args()
+    a = argparse.Namespace(steps=steps, size=size, fd=fd)
     L = a.size
     st = setup("f32", L, L / 4)
     w_t = smooth_field(L, L, 1, 0.02)
@@ -124,7 +122,16 @@ def main():
         out["fd_fp64"] = checks
         out["fp32_vs_fp64_grad_rel_l2"] = float(np.linalg.norm(gw - gw64) / np.linalg.norm(gw64))
         out["fp32_vs_fp64_kappa_rel"] = abs(gk - gk64) / abs(gk64)
-    print(json.dumps(out))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--size", type=int, default=96)
+    ap.add_argument("--fd", action="store_true")
+    a = ap.parse_args()
+    print(json.dumps(measure(a.steps, a.size, a.fd)))
 
 
 if __name__ == "__main__":

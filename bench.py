@@ -18,6 +18,7 @@ when that build is absent -- on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import importlib
 import json
 import os
 import statistics
@@ -313,6 +314,12 @@ def run_ours(args) -> None:
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_sample(args, wl)
+    s.close()
+    # ---- the targets' other terms, measured in the same run outside the timed
+    # region (rank 0, the default FUSED FP16 line only)
+    targets = None
+    if rank == 0 and not args.no_targets and args.scheme == "fused" and args.storage == "f16":
+        targets = target_terms(args, wl, cp, torch, local, value)
     if rank == 0:
         line = {
             "metric": metric_name(args), "value": round(value, 1), "unit": "MLUPS", "n_gpus": ws,
@@ -326,13 +333,47 @@ def run_ours(args) -> None:
                        "l2": "state larger than L2 (no flush needed)" if n * 44 > 129e6
                              else "state fits in L2; numbers are L2-resident"},
             "gpu_launches": launches, "clocks": clk, "roofline": roofline, "e2e": e2e,
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "targets": targets,
         }
         print(json.dumps(line))
-    s.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def target_terms(args, wl: dict, cp, torch, device: int, fused_mlups: float) -> dict:
+    """The other terms of the benchmark's targets, each on its own workload:
+    the PLAIN FP32 form of the same box (the FP16-storage fused solver's
+    target is >= 2x its MLUPS), and the adjoint-over-forward time of the
+    wall-field inversion set-up (96^3 CS box, FP32; target <= 3x) against both
+    the PLAIN forward it differentiates and the FUSED FP32 forward."""
+    out = {}
+    s = make_solver(cp, wl, "plain", "f32", device)
+    stream = torch.cuda.ExternalStream(s.stream)
+    s.step(3)
+    s.sync()
+    k = max(5, min(args.steps, 20))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(k)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    plain = s.n / (ms / 1e3) / 1e6
+    s.close()
+    out["plain_f32"] = {"value": round(plain, 1), "unit": "MLUPS", "ms_per_step": round(ms, 4), "steps": k,
+                        "workload": wl["name"]}
+    out["fused_f16_over_plain_f32"] = round(fused_mlups / plain, 3)
+    ab = importlib.import_module("3dcpmpmodel_gb300.adjoint_bench")
+    steps = 400
+    r = ab.measure(steps=steps, size=96)
+    out["adjoint"] = {"workload": "wall-field inversion, 96^3 CS T/Tc 0.8, FP32", "steps": steps,
+                      "checkpoint_every": int(np.ceil(np.sqrt(steps))),
+                      "adjoint_s": r["adjoint_s"], "forward_plain_f32_s": r["forward_s"],
+                      "forward_fused_f32_s": r["forward_fused_f32_s"],
+                      "adjoint_over_plain_forward": r["value"],
+                      "adjoint_over_fused_forward": r["adjoint_over_fused_forward"]}
+    return out
 
 
 def c4_params(cp, storage: str, seed: int = 0, count: int = 96):
@@ -597,6 +638,8 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=2_000_000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-targets", action="store_true",
+                    help="skip the PLAIN FP32 and adjoint sub-measurements of the default line")
     ap.add_argument("--tile", default="",
                     help="ty,tz,xl[,np[,form]]: this fused tile (form 1: the two-pass step) instead of the "
                          "autotuner's")
