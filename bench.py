@@ -316,9 +316,9 @@ def run_ours(args) -> None:
         cpu = cpu_sample(args, wl)
     s.close()
     # ---- the targets' other terms, measured in the same run outside the timed
-    # region (rank 0, the default FUSED FP16 line only)
+    # region (one GPU, the default FUSED FP16 line only)
     targets = None
-    if rank == 0 and not args.no_targets and args.scheme == "fused" and args.storage == "f16":
+    if ws == 1 and not args.no_targets and args.scheme == "fused" and args.storage == "f16":
         targets = target_terms(args, wl, cp, torch, local, value)
     if rank == 0:
         line = {
