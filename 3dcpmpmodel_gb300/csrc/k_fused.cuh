@@ -169,6 +169,39 @@ __device__ __forceinline__ float2 load_pair<__nv_bfloat16>(const __nv_bfloat16 *
                 : make_float2(__bfloat162float(ptr[0]), __bfloat162float(ptr[1]));
 }
 
+// Two stored values of consecutive nodes kept packed (one register for FP16
+// and BF16) from the load until the decode, and their conversion to floats
+// (exact, the same floats as load_pair's).
+template <class S>
+struct Packed;
+template <>
+struct Packed<__half> {
+    using T = __half2;
+    static __device__ __forceinline__ T load(const __half *p, bool even)
+    {
+        return even ? *reinterpret_cast<const __half2 *>(p) : __halves2half2(p[0], p[1]);
+    }
+    static __device__ __forceinline__ float2 tof(T v) { return __half22float2(v); }
+};
+template <>
+struct Packed<__nv_bfloat16> {
+    using T = __nv_bfloat162;
+    static __device__ __forceinline__ T load(const __nv_bfloat16 *p, bool even)
+    {
+        return even ? *reinterpret_cast<const __nv_bfloat162 *>(p) : __halves2bfloat162(p[0], p[1]);
+    }
+    static __device__ __forceinline__ float2 tof(T v) { return __bfloat1622float2(v); }
+};
+template <>
+struct Packed<float> {
+    using T = float2;
+    static __device__ __forceinline__ T load(const float *p, bool even)
+    {
+        return even ? *reinterpret_cast<const float2 *>(p) : make_float2(p[0], p[1]);
+    }
+    static __device__ __forceinline__ float2 tof(T v) { return v; }
+};
+
 // Is node k of a column one whose 18 sources are fluid nodes with no z wrap?
 __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
 {
@@ -192,13 +225,16 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
     // an immediate
     const int plane = p.dy * p.dz;
     const float *fI = f0 + I;
-    float2 hv[Q - 1], a[Q - 1];
+    // the moving populations stay packed until the decode, so the 18 pairs and
+    // the anchors fit the register budget without reloads
+    typename Packed<S>::T hv[Q - 1];
+    float2 a[Q - 1];
 #pragma unroll
     for (int q = 1; q < Q; ++q) {
         const int off = cx(q) * plane + cy(q) * p.dz + cz(q);
         const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, I) - off;
         const bool odd_off = (cz(q) & 1) != 0;
-        hv[q - 1] = load_pair<S>(hp, EVEN && (P == 0 || !odd_off));
+        hv[q - 1] = Packed<S>::load(hp, EVEN && (P == 0 || !odd_off));
         if (!EVEN) a[q - 1] = load_pair<float>(fI - off, false);
     }
     if (EVEN) {
@@ -239,7 +275,7 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
     }
     float2 g[Q];
 #pragma unroll
-    for (int q = 1; q < Q; ++q) g[q] = Lane2::fma(Lane2::k(3.f), a[q - 1], hv[q - 1]);
+    for (int q = 1; q < Q; ++q) g[q] = Lane2::fma(Lane2::k(3.f), a[q - 1], Packed<S>::tof(hv[q - 1]));
     float2 ES, DS;
     mass_sums<Lane2>(g, ES, DS);
     const float2 a0 = *reinterpret_cast<const float2 *>(f0 + I);
