@@ -84,8 +84,7 @@ struct cpmp_batch {
     BatchBox *d_boxes = nullptr;
     unsigned *d_counter = nullptr;
     unsigned *d_mvmax = nullptr;  // [2][boxes]: each box's max |MV|^2 of its last collision, per parity
-    long long total_items = 0, nodes = 0, max_cols = 0, max_pairs = 0, launches = 0;
-    int max_dx = 0;
+    long long total_items = 0, nodes = 0, wall_blocks = 0, density_blocks = 0, launches = 0;
     cudaGraphExec_t gexec = nullptr;
     std::unique_ptr<LaunchHook> hook;
     bool timing = false;
@@ -1040,11 +1039,8 @@ cpmp_status batch_upload(cpmp_batch *b)
     const int nb = (int)b->boxes.size();
     std::vector<KParams<float>> kp(nb);
     std::vector<BatchBox> bx(nb);
-    long long item = 0;
+    long long item = 0, wblk = 0, dblk = 0;
     b->nodes = 0;
-    b->max_dx = 0;
-    b->max_cols = 0;
-    b->max_pairs = 0;
     for (int i = 0; i < nb; ++i) {
         cpmp_handle *h = b->boxes[i];
         kp[i] = make_kparams<float>(h);
@@ -1058,12 +1054,17 @@ cpmp_status batch_upload(cpmp_batch *b)
         bx[i].tiles_y = (h->p.dy + b->tile.ty - 1) / b->tile.ty;
         bx[i].item0 = item;
         item += (long long)bx[i].tiles_z * bx[i].tiles_y * ((h->p.dx + b->tile.xl - 1) / b->tile.xl);
+        // flattened wall and density grids: the box's blocks follow the previous box's
+        bx[i].wblk0 = wblk;
+        if (h->p.wall_mode == 1) wblk += ((long long)h->p.dx * h->p.dy + BATCH_WALL_BLOCK - 1) / BATCH_WALL_BLOCK;
+        bx[i].dblk0 = dblk;
+        dblk += (((long long)h->p.dy * pairs_per_column(h->p.dz) + BATCH_DENSITY_BLOCK - 1) / BATCH_DENSITY_BLOCK) *
+                h->p.dx;
         b->nodes += h->n;
-        b->max_dx = std::max(b->max_dx, h->p.dx);
-        b->max_cols = std::max(b->max_cols, (long long)h->p.dx * h->p.dy);
-        b->max_pairs = std::max(b->max_pairs, (long long)h->p.dy * ((h->p.dz + 1) / 2));
     }
     b->total_items = item;
+    b->wall_blocks = wblk;
+    b->density_blocks = dblk;
     CK(cudaMemcpyAsync(b->d_params, kp.data(), nb * sizeof(KParams<float>), cudaMemcpyHostToDevice, b->st));
     CK(cudaMemcpyAsync(b->d_boxes, bx.data(), nb * sizeof(BatchBox), cudaMemcpyHostToDevice, b->st));
     CK(cudaStreamSynchronize(b->st));
@@ -1076,7 +1077,7 @@ void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
     const size_t nb = b->boxes.size();
     cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
     fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params, b->d_boxes,
-                     (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P, b->d_counter, b->st, hook);
+                     (int)b->boxes.size(), b->total_items, b->wall_blocks, b->density_blocks, P, b->d_counter, b->st, hook);
     if (!bookkeeping) return;
     for (cpmp_handle *h : b->boxes) {
         h->step += 1;
@@ -1214,7 +1215,7 @@ cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
                 const size_t nb = b->boxes.size();
                 cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
                 fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params,
-                                 b->d_boxes, (int)b->boxes.size(), b->total_items, b->max_dx, b->max_cols, b->max_pairs, P,
+                                 b->d_boxes, (int)b->boxes.size(), b->total_items, b->wall_blocks, b->density_blocks, P,
                                  b->d_counter, b->st, nullptr);
             }
             cudaError_t e = cudaStreamEndCapture(b->st, &g);

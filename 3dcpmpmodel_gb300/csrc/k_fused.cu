@@ -95,16 +95,19 @@ __global__ void __launch_bounds__(256) k_velocity(KParams<float> p, int P, const
     u[I + 2 * p.n] = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) / r;
 }
 
-// All boxes of a batch: blockIdx.y = box; the wall of box b at parity P is
+// All boxes of a batch on one flattened grid (box b owns the blocks from
+// boxes[b].wblk0 on, none for a periodic box); the wall of box b at parity P is
 // computed on rho[P] and mirrored into rho[1-P].
 __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
-                                  int pass, int P)
+                                  int nbox, int pass, int P)
 {
-    const KParams<float> &p = params[blockIdx.y];
+    const long long g = blockIdx.x;
+    const int bi = batch_box_of(boxes, nbox, g, [](const BatchBox &x) { return x.wblk0; });
+    const KParams<float> &p = params[bi];
     if (p.wall_mode != 1) return;
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const BatchBox &b = boxes[bi];
+    const long long c = (g - b.wblk0) * blockDim.x + threadIdx.x;
     if (c >= (long long)p.dx * p.dy) return;
-    const BatchBox &b = boxes[blockIdx.y];
     wall_column<float>(p, pass, c, b.rho[P], nullptr, b.rho[1 - P]);
 }
 
@@ -333,14 +336,13 @@ void batch_collide_l(const FusedTile &t, const KParams<float> *params, const Bat
 
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter,
+                      long long wall_blocks, long long density_blocks, int P, unsigned *counter,
                       cudaStream_t st, LaunchHook *hook)
 {
-    if (wall_mode == 1) {
-        const dim3 gw((unsigned)((max_cols + 127) / 128), (unsigned)nbox);
+    if (wall_mode == 1 && wall_blocks > 0) {
         for (int s = 0; s < (complex_bc ? 3 : 1); ++s) {
             hook_begin(hook, K_WALL, st);
-            k_wall_pass_batch<<<gw, 128, 0, st>>>(params, boxes, s, P);
+            k_wall_pass_batch<<<(unsigned)wall_blocks, BATCH_WALL_BLOCK, 0, st>>>(params, boxes, nbox, s, P);
             hook_end(hook, K_WALL, st);
         }
     }
@@ -357,8 +359,7 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {
         using S = decltype(tag);
-        const dim3 gd((unsigned)((max_pairs + 127) / 128), (unsigned)max_dx, (unsigned)nbox);
-        k_density_batch<S><<<gd, 128, 0, st>>>(params, boxes, 1 - P);
+        k_density_batch<S><<<(unsigned)density_blocks, BATCH_DENSITY_BLOCK, 0, st>>>(params, boxes, nbox, 1 - P);
     });
     hook_end(hook, K_DENSITY, st);
 }

@@ -214,10 +214,14 @@ __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
 // index and N even, so it is that of cz(q)) and aligned pairs are vector
 // loads; otherwise all moving-population and anchor loads are scalar.  Every
 // load is issued before the first add so their latencies overlap.
+// botw / topw (even DZ only): the pair is (2, 3) / (dz-4, dz-3) of an x/y-
+// interior column of a walled box: its fluid node's sources across the wall
+// layer are its own slots and rest population (density_wall_node's sums, by
+// selects instead of a per-node path), and only the fluid node is written.
 template <class S, int P, bool EVEN, class SL>
 __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const SL &slots,
                                                   const float *__restrict__ f0, float *__restrict__ rho,
-                                                  unsigned I)
+                                                  unsigned I, bool botw = false, bool topw = false)
 {
     // node indices are 32-bit (the FUSED scheme keeps N below 2^32); the
     // neighbour offsets are applied as signed pointer offsets from the node's
@@ -235,6 +239,9 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
         const S *hp = P == 0 ? slots(q - 1, I) : slots(opp(q) - 1, I) - off;
         const bool odd_off = (cz(q) & 1) != 0;
         hv[q - 1] = Packed<S>::load(hp, EVEN && (P == 0 || !odd_off));
+        // a source on a wall layer: the node's own slot (half-way bounce-back)
+        if (EVEN && P == 1 && cz(q) == 1 && botw) hv[q - 1] = Packed<S>::load(slots(q - 1, I), true);
+        if (EVEN && P == 1 && cz(q) == -1 && topw) hv[q - 1] = Packed<S>::load(slots(q - 1, I), true);
         if (!EVEN) a[q - 1] = load_pair<float>(fI - off, false);
     }
     if (EVEN) {
@@ -272,6 +279,13 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
         for (int q = 1; q < Q; ++q)  // in-plane diagonals: cz = 0 only
             if (cz(q) == 0 && cx(q) != 0 && cy(q) != 0)
                 a[q - 1] = *reinterpret_cast<const float2 *>(fI - (cx(q) * plane + cy(q) * p.dz));
+        // a source on a wall layer: the node's own rest population
+        const float2 own = *reinterpret_cast<const float2 *>(fI);
+#pragma unroll
+        for (int q = 1; q < Q; ++q) {
+            if (cz(q) == 1 && botw) a[q - 1] = own;
+            if (cz(q) == -1 && topw) a[q - 1] = own;
+        }
     }
     float2 g[Q];
 #pragma unroll
@@ -279,7 +293,10 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
     float2 ES, DS;
     mass_sums<Lane2>(g, ES, DS);
     const float2 a0 = *reinterpret_cast<const float2 *>(f0 + I);
-    *reinterpret_cast<float2 *>(rho + I) = Lane2::add(a0, Lane2::div_rn(Lane2::fma(Lane2::k(2.f), ES, DS), 36.f));
+    const float2 r = Lane2::add(a0, Lane2::div_rn(Lane2::fma(Lane2::k(2.f), ES, DS), 36.f));
+    if (botw) rho[I + 1] = r.y;       // node I is on the bottom wall layer
+    else if (topw) rho[I] = r.x;      // node I + 1 is on the top wall layer
+    else *reinterpret_cast<float2 *>(rho + I) = r;
 }
 
 // Density of one fluid node k of an x/y-interior column of a walled box
@@ -347,6 +364,16 @@ __device__ __forceinline__ void density_pair(const KParams<float> &p, int P, con
 {
     const bool in0 = k0 >= 0 && k0 < p.dz, in1 = k0 + 1 >= 0 && k0 + 1 < p.dz;
     const bool xy = i >= 1 && i + 1 < p.dx && j >= 1 && j + 1 < p.dy;
+    if ((p.dz & 1) == 0 && p.wall_mode == 1 && xy) {
+        // every pair of an x/y-interior column of a walled box with even DZ
+        // (k0 even): the wall-adjacent pairs take the paired path with selects
+        if (k0 < 2 || k0 > p.dz - 4) return;  // both nodes on wall layers
+        const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
+        const bool botw = k0 == 2, topw = k0 == p.dz - 4;
+        if (P == 0) density_pair_fast<S, 0, true>(p, slots, f0, rho, I, botw, topw);
+        else density_pair_fast<S, 1, true>(p, slots, f0, rho, I, botw, topw);
+        return;
+    }
     const bool fast = in0 && in1 && xy && z_plain(p, k0) && z_plain(p, k0 + 1);
     if (!fast) {
         const unsigned I = ((unsigned)i * p.dy + j) * p.dz + k0;
@@ -383,12 +410,26 @@ __device__ __forceinline__ int pair_k0(const KParams<float> &p, int i, int j, in
     const long long base = ((long long)i * p.dy + j) * p.dz;
     return 2 * t - (int)(base & 1);
 }
-__host__ __device__ __forceinline__ int pairs_per_column(int dz) { return (dz + 1) / 2; }
+
+// The box of block g of a batch's flattened grid: the last box whose first
+// block (first(box)) is at most g; boxes with no blocks share the next box's
+// first block and are skipped.
+template <class F>
+__device__ __forceinline__ int batch_box_of(const BatchBox *__restrict__ boxes, int nbox, long long g, F first)
+{
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first(boxes[mid]) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 
 // Block: 32 pairs of a column x 4 columns (y); grid (pair blocks, y blocks,
 // dx).  The anchors of the y +- 1 neighbours of a block's nodes are mostly
 // rows that the same block reads, so they come from L1.
-constexpr int DENSITY_BZ = 32, DENSITY_BY = 4;
 template <class S>
 __global__ void __launch_bounds__(DENSITY_BZ *DENSITY_BY, 8) k_density(KParams<float> p, int P,
                                                                      const S *__restrict__ h,
@@ -849,17 +890,26 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
 // plane's pairs (numbered column by column) in blocks of 128; blocks past a
 // box's extent exit at once.
 template <class S>
-__global__ void __launch_bounds__(128, 8) k_density_batch(const KParams<float> *__restrict__ params,
-                                                       const BatchBox *__restrict__ boxes, int P)
+__global__ void __launch_bounds__(BATCH_DENSITY_BLOCK, 8) k_density_batch(const KParams<float> *__restrict__ params,
+                                                                        const BatchBox *__restrict__ boxes, int nbox,
+                                                                        int P)
 {
-    const int b = blockIdx.z, i = blockIdx.y;
+    // flattened grid: box b owns the blocks from boxes[b].dblk0 on, for each
+    // x plane ceil(dy * pairs per column / BATCH_DENSITY_BLOCK) of them; the
+    // pairs of a plane are numbered column by column, so a block's threads
+    // cover consecutive pairs of one or more columns (no idle lanes on short
+    // columns)
+    const long long g = blockIdx.x;
+    const int b = batch_box_of(boxes, nbox, g, [](const BatchBox &x) { return x.dblk0; });
     const KParams<float> &p = params[b];
-    if (i >= p.dx) return;
-    const int per_col = pairs_per_column(p.dz);
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= p.dy * per_col) return;
     const BatchBox &bx = boxes[b];
-    const int j = e / per_col, t = e - j * per_col;
+    const int ppc = pairs_per_column(p.dz);
+    const int per_plane = (int)(((long long)p.dy * ppc + BATCH_DENSITY_BLOCK - 1) / BATCH_DENSITY_BLOCK);
+    const long long local = g - bx.dblk0;
+    const int i = (int)(local / per_plane);
+    const int e = (int)(local - (long long)i * per_plane) * BATCH_DENSITY_BLOCK + threadIdx.x;
+    if (e >= p.dy * ppc) return;
+    const int j = e / ppc, t = e - j * ppc;
     density_pair<S>(p, P, (const S *)bx.h, SlotBase<const S>{(const S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.rho[P], i,
                     j, pair_k0(p, i, j, t));
 }

@@ -107,12 +107,12 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 // One time step of every box of a batch: batched wall passes, the persistent
 // fused collide over all (box, tile, chunk) work items, the batched density
 // pass.  params/boxes are device arrays of nbox entries; counter is one
-// device unsigned (reset here); max_dx / max_cols bound the boxes' x extent
-// and wall columns, max_pairs the density pass's node pairs per x plane
-// (dy * ((dz + 1) / 2)).
+// device unsigned (reset here); wall_blocks / density_blocks are the sizes of
+// the flattened wall and density grids (each box's first block in
+// BatchBox::wblk0 / dblk0).
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      int max_dx, long long max_cols, long long max_pairs, int P, unsigned *counter,
+                      long long wall_blocks, long long density_blocks, int P, unsigned *counter,
                       cudaStream_t st, LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).

@@ -104,6 +104,15 @@ inline void hook_end(LaunchHook *h, int cls, cudaStream_t st)
     if (h->pending.size() > 4096) h->fold();
 }
 
+// Node pairs per z column of the density pass (an odd DZ adds a lone node);
+// its block: DENSITY_BZ pairs along z x DENSITY_BY rows; the batched density
+// pass: BATCH_DENSITY_BLOCK consecutive pairs of an x plane per block; the
+// batched wall pass: BATCH_WALL_BLOCK columns per block.
+__host__ __device__ inline int pairs_per_column(int dz) { return (dz + 1) / 2; }
+constexpr int DENSITY_BZ = 32, DENSITY_BY = 4;
+constexpr int BATCH_DENSITY_BLOCK = 128;
+constexpr int BATCH_WALL_BLOCK = 128;
+
 // Buffers of one box of a batch (the KParams of every box live in a device
 // array next to these).
 struct BatchBox {
@@ -111,6 +120,8 @@ struct BatchBox {
     float *f0[2];
     float *rho[2];         // rho[0] is the density read at even steps
     long long item0;       // first collide work item of this box
+    long long wblk0;       // first block of this box in the flattened wall-pass grid
+    long long dblk0;       // first block of this box in the flattened density-pass grid
     int tiles_z, tiles_y;  // column tiles per x plane
 };
 

@@ -161,6 +161,23 @@ def test_mass_conservation(cpmp, scheme, storage):
     s.close()
 
 
+@pytest.mark.parametrize("cfg", [WALLED, dict(WALLED, dz=27), PERIODIC_CS], ids=["walled", "walled_odd_dz", "periodic"])
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_density_pass_equals_population_sum(cpmp, cfg, storage):
+    """The FUSED density field (the density pass, with its paired, wall-pair
+    and edge paths) equals the sum of the decoded post-stream populations of
+    every fluid node, after steps of both A-A parities."""
+    s = solver_for(cpmp, cfg, scheme="fused", storage=storage)
+    fluid = s.get("type") == 1
+    for steps in (7, 1):
+        s.step(steps)
+        d = s.get("dist").reshape(19, -1)
+        rho = s.get("rho")
+        err = np.max(np.abs(d.sum(0)[fluid] - rho[fluid]) / rho[fluid])
+        assert err < 2e-6, (steps, err)
+    s.close()
+
+
 def test_step_chunking_is_invisible(cpmp):
     """Graph replay (2-step chunks) and single launches give the same state."""
     a = solver_for(cpmp, WALLED, scheme="fused", storage="f16")
