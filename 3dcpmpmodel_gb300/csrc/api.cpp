@@ -1083,7 +1083,7 @@ void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
         h->step += 1;
         std::swap(h->rho, h->rho2);
     }
-    b->launches += (b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2;
+    b->launches += (b->wall_mode == 1 ? 1 : 0) + 2;
 }
 
 cpmp_status batch_check(cpmp_batch *b)
@@ -1230,7 +1230,7 @@ cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
         while (left >= 2) {
             CK(cudaGraphLaunch(b->gexec, b->st));
             for (cpmp_handle *h : b->boxes) h->step += 2;  // two swaps: rho pointers unchanged
-            b->launches += 2LL * ((b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2);
+            b->launches += 2LL * ((b->wall_mode == 1 ? 1 : 0) + 2);
             left -= 2;
         }
     }
@@ -1347,7 +1347,7 @@ cpmp_status cpmp_batch_autotune(cpmp_batch *b, int *tile_y, int *tile_z, int *ma
             if (err != cudaSuccess) break;
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
-            b->launches += 3LL * ((b->wall_mode == 1 ? (b->complex_bc ? 3 : 1) : 0) + 2);
+            b->launches += 3LL * ((b->wall_mode == 1 ? 1 : 0) + 2);
             if (ms / 2 < best_ms) {
                 best_ms = ms / 2;
                 best = b->tile;

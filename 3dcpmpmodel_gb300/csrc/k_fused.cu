@@ -95,11 +95,58 @@ __global__ void __launch_bounds__(256) k_velocity(KParams<float> p, int P, const
     u[I + 2 * p.n] = (f[5] + f[11] + f[12] + f[15] + f[16] - f[6] - f[13] - f[14] - f[17] - f[18]) / r;
 }
 
+// The layered wall passes of wall_column (pass 0: layers 0-2 <- E(layer 3);
+// pass 1: layer 1 <- E(layer 2); pass 2: layer 0 <- E(layer 1), the same at
+// the top wall) in one launch: E at a column reads layer 3 at the column and
+// its four xy-diagonal neighbours, so the second layer of a column needs E at
+// 5 columns and the third at 13, within a radius-3 diagonal neighbourhood.
+// Every value is the expression of wall_extrap on the same inputs, so the
+// result is that of the three launches bit for bit.  FUSED scheme: density
+// only, mirrored into the other density buffer.  Used by the batches (many
+// small boxes: one launch instead of three is faster there).
+__device__ __forceinline__ float wall_mix(float c, float mm, float mp, float pm, float pp)
+{
+    // wall_extrap's sum order: centre x 2, then (-,-), (-,+), (+,-), (+,+)
+    return (c * 2.f + mm + mp + pm + pp) / 6.f;
+}
+__device__ __forceinline__ void wall_column_all(const KParams<float> &p, long long c, float *rho, float *mirror)
+{
+    const int i = (int)(c / p.dy), j = (int)(c - (c / p.dy) * p.dy);
+    const int D = p.dz;
+    auto wr = [](int a, int n) { a %= n; return a < 0 ? a + n : a; };
+    for (int top = 0; top < 2; ++top) {
+        const int k3 = top ? D - 4 : 3, step = top ? 1 : -1;  // layers k3 + step, + 2 step, + 3 step
+        auto E = [&](int a, int b) { return wall_extrap<float>(p, rho, wr(i + a, p.dx), wr(j + b, p.dy), k3); };
+        const float e00 = E(0, 0);
+        float l1 = e00, l0 = e00;
+        if (p.complex_bc) {
+            const float emm = E(-1, -1), emp = E(-1, 1), epm = E(1, -1), epp = E(1, 1);
+            const float e2mm = E(-2, -2), e2m0 = E(-2, 0), e0m2 = E(0, -2), e2mp = E(-2, 2), e0p2 = E(0, 2);
+            const float e2pm = E(2, -2), e2p0 = E(2, 0), e2pp = E(2, 2);
+            l1 = wall_mix(e00, emm, emp, epm, epp);
+            const float lmm = wall_mix(emm, e2mm, e2m0, e0m2, e00);
+            const float lmp = wall_mix(emp, e2m0, e2mp, e00, e0p2);
+            const float lpm = wall_mix(epm, e0m2, e00, e2pm, e2p0);
+            const float lpp = wall_mix(epp, e00, e0p2, e2p0, e2pp);
+            l0 = wall_mix(l1, lmm, lmp, lpm, lpp);
+        }
+        const long long col = ((long long)i * p.dy + j) * D;
+        const long long k_e = col + k3 + step, k_1 = col + k3 + 2 * step, k_0 = col + k3 + 3 * step;
+        rho[k_e] = e00;
+        rho[k_1] = l1;
+        rho[k_0] = l0;
+        if (mirror) {
+            mirror[k_e] = e00;
+            mirror[k_1] = l1;
+            mirror[k_0] = l0;
+        }
+    }
+}
 // All boxes of a batch on one flattened grid (box b owns the blocks from
 // boxes[b].wblk0 on, none for a periodic box); the wall of box b at parity P is
 // computed on rho[P] and mirrored into rho[1-P].
 __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
-                                  int nbox, int pass, int P)
+                                  int nbox, int P)
 {
     const long long g = blockIdx.x;
     const int bi = batch_box_of(boxes, nbox, g, [](const BatchBox &x) { return x.wblk0; });
@@ -108,7 +155,7 @@ __global__ void k_wall_pass_batch(const KParams<float> *__restrict__ params, con
     const BatchBox &b = boxes[bi];
     const long long c = (g - b.wblk0) * blockDim.x + threadIdx.x;
     if (c >= (long long)p.dx * p.dy) return;
-    wall_column<float>(p, pass, c, b.rho[P], nullptr, b.rho[1 - P]);
+    wall_column_all(p, c, b.rho[P], b.rho[1 - P]);
 }
 
 // ------------------------------------------------------------- dispatch ----
@@ -245,6 +292,8 @@ void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d
 void fused_launch_wall(const KParams<float> &p, float *rho, float *rho_mirror, cudaStream_t st, LaunchHook *hook)
 {
     if (p.wall_mode != 1) return;
+    // one launch per layer pass: at 512^3 the single-launch form (k_wall_pass_batch's
+    // wall_column_all) is slower, its redundant layer-3 reads cost more than two launches
     const long long np = (long long)p.dx * p.dy;
     const unsigned gw = (unsigned)((np + 127) / 128);
     for (int s = 0; s < (p.complex_bc ? 3 : 1); ++s) {
@@ -340,11 +389,9 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
                       cudaStream_t st, LaunchHook *hook)
 {
     if (wall_mode == 1 && wall_blocks > 0) {
-        for (int s = 0; s < (complex_bc ? 3 : 1); ++s) {
-            hook_begin(hook, K_WALL, st);
-            k_wall_pass_batch<<<(unsigned)wall_blocks, BATCH_WALL_BLOCK, 0, st>>>(params, boxes, nbox, s, P);
-            hook_end(hook, K_WALL, st);
-        }
+        hook_begin(hook, K_WALL, st);
+        k_wall_pass_batch<<<(unsigned)wall_blocks, BATCH_WALL_BLOCK, 0, st>>>(params, boxes, nbox, P);
+        hook_end(hook, K_WALL, st);
     }
     hook_begin(hook, K_FUSED, st);
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
