@@ -883,6 +883,10 @@ cpmp_status cpmp_autotune(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
     for (int t = 0; t < fused_tile_count(); ++t) {
         for (int xi = 0; xi < 5; ++xi) {
             FusedTile ft = fused_tile(t, xls[xi]);
+            // the two-pass form is slower in steady state on every workload
+            // measured, while timing its two kernels back to back on the
+            // scratch copy underestimates it; it is selected explicitly only
+            if (ft.form != 0) continue;
             if (!fused_tile_usable(h->p.storage, h->p.lap_order, ft.ty, ft.tz, ft.np, ft.form)) continue;
             if (ft.np == 2 && !pair_grid_ok(h->p.dz)) continue;
             if (ft.xl > h->p.dx && xi > 0) continue;

@@ -239,7 +239,9 @@ cpmp_status cpmp_get_tile(cpmp_handle *h, int *tile_y, int *tile_z, int *march_x
  *                       the K1/K2 term) and a collide-stream pass without
  *                       shared memory; node pairs (nodes_per_thread 2), DZ a
  *                       multiple of 4, the column tile is the force pass's.
- * cpmp_autotune times both forms; cpmp_set_tile_ex selects the one-pass form. */
+ * cpmp_autotune times the one-pass tiles only (the two-pass form is slower in
+ * steady state on every workload measured); cpmp_set_tile_ex selects the
+ * one-pass form. */
 enum { CPMP_FORM_ONE_PASS = 0, CPMP_FORM_TWO_PASS = 1 };
 cpmp_status cpmp_set_tile_form(cpmp_handle *h, int tile_y, int tile_z, int march_x, int nodes_per_thread,
                                int form);
