@@ -434,14 +434,12 @@ void diag_launch_mv(const uint8_t *type, const float *rho, const float *u, const
 // Partials of cpmp_mass_noalloc live in this file-scope device array instead
 // of a buffer the handle allocates.  Host code cannot use the array's name as
 // an address (it is a host-side stand-in); the device address comes from
-// cudaGetSymbolAddress with the device current.  It is looked up again on
-// every call made outside stream capture (the lookup allocates nothing and
-// follows the module if a device reset or a new primary context reloaded it
-// at another address); a call made while its stream is capturing uses the
-// address the last uncaptured call on that device saw, and fails if there
-// was none.  Each call writes every partial triple it later reads, so nothing
-// has to be cleared between calls; calls that overlap on the GPU share the
-// array and race.
+// cudaGetSymbolAddress with the device current, on the first call on a
+// device (which has to come before any stream capture) and again on later
+// calls (the lookup allocates nothing and follows the module if a device
+// reset or a new primary context reloaded it at another address).  Each call
+// writes every partial triple it later reads, so nothing has to be cleared
+// between calls; calls that overlap on the GPU share the array and race.
 static __device__ __align__(256) double g_noalloc_partials[3 * kMaxRedBlocks];
 
 namespace {

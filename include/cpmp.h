@@ -364,12 +364,11 @@ void cpmp_batch_destroy(cpmp_batch *b);
  * live in a fixed 24 KB device array inside the library (1024 partial
  * triples; every GPU that loads the library holds it until the process
  * exits), so every n from 1 to CPMP_NOALLOC_MAX_NODES fits and larger n is
- * rejected with CPMP_ERR_SIZE.  Each call outside stream capture looks up
- * that array's device address (cudaGetSymbolAddress, no allocation), so a
- * device reset between calls is harmless; a call on a capturing stream
- * reuses the address of the last uncaptured call on its device and fails
- * with CPMP_ERR_CUDA if there was none, so make one call before capturing.
- * All calls share the array: calls that overlap on the GPU (e.g. on two
+ * rejected with CPMP_ERR_SIZE.  The first call on a device looks up that
+ * array's device address there (cudaGetSymbolAddress, no allocation), with
+ * that device current; make that first call before any stream capture.  Later
+ * calls look the address up again, so a device reset between calls is
+ * harmless.  All calls share the array: calls that overlap on the GPU (e.g. on two
  * streams at once) race and give wrong results; each call writes every
  * partial it reads, so nothing carries over between calls that follow one
  * another. */
