@@ -5,6 +5,7 @@
 // then shared memory, in a fixed order, so results are run-to-run identical.
 #include <cfloat>
 #include <climits>
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -16,6 +17,10 @@ namespace cpmp {
 namespace {
 constexpr int kRedThreads = 256;
 constexpr int kMaxRedBlocks = 1024;
+// Blocks of a reduction over a large box: 6 on each of the 152 SMs (48 warps
+// per SM), so that every SM gets the same share of a grid-stride pass.
+constexpr int kRedBlocks = 912;
+static_assert(kRedBlocks <= kMaxRedBlocks, "partial arrays hold kMaxRedBlocks triples");
 
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -52,54 +57,132 @@ __device__ __forceinline__ int warp_max_i(int v)
 int diag_partial_blocks(long long n)
 {
     long long b = (n + kRedThreads - 1) / kRedThreads;
-    if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+    if (b > kRedBlocks) b = kRedBlocks;
     if (b < 1) b = 1;
     return (int)b;
 }
 
+namespace {
+// vec flags of k_mass_partial: bit 0 when n is a multiple of 4 with type
+// 4-byte and rho 16-byte aligned, bit 1 when MV is 16-byte aligned as well.
+int mass_vec_flags(const void *type, const void *rho, const void *mv, long long n)
+{
+    if (n % 4 != 0 || (reinterpret_cast<uintptr_t>(type) & 3) || (reinterpret_cast<uintptr_t>(rho) & 15)) return 0;
+    return 1 | ((mv && !(reinterpret_cast<uintptr_t>(mv) & 15)) ? 2 : 0);
+}
+}  // namespace
+
+// Running sums of one thread of the mass pass.  FP32 fields: the sum is an
+// exact FP32 pair (TwoSum: hi + lo equals the sum of the values added, up to
+// the rounding of lo), so the FP64 pipe -- a small fraction of the FP32 rate
+// on this part -- only joins the threads' partials; the sign test and |MV|^2
+// stay in FP32 as the fields are.  FP64 fields: plain FP64 sums.
 template <class R>
-__global__ void __launch_bounds__(kRedThreads) k_mass_partial(const uint8_t *__restrict__ type,
+struct MassAcc {
+    double s = 0.0, m2 = 0.0;
+    int bad = 0;
+    __device__ __forceinline__ void add(double d)
+    {
+        if (!(d >= 0.0)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
+        s += d;
+    }
+    __device__ __forceinline__ void speed(double a, double b, double c) { m2 = fmax(m2, a * a + b * b + c * c); }
+    __device__ __forceinline__ double sum() const { return s; }
+    __device__ __forceinline__ double max2() const { return m2; }
+};
+template <>
+struct MassAcc<float> {
+    float hi = 0.f, lo = 0.f, m2 = 0.f;
+    int bad = 0;
+    __device__ __forceinline__ void add(float d)
+    {
+        if (!(d >= 0.f)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
+        const float t = hi + d, bp = t - hi;
+        lo += (hi - (t - bp)) + (d - bp);
+        hi = t;
+    }
+    __device__ __forceinline__ void speed(float a, float b, float c) { m2 = fmaxf(m2, fmaf(a, a, fmaf(b, b, c * c))); }
+    __device__ __forceinline__ double sum() const { return (double)hi + (double)lo; }
+    __device__ __forceinline__ double max2() const { return (double)m2; }
+};
+
+// Four consecutive values of a field starting at node 4g (16-byte aligned).
+__device__ __forceinline__ void load4(const float *__restrict__ p, long long g, float (&v)[4])
+{
+    const float4 t = reinterpret_cast<const float4 *>(p)[g];
+    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+}
+__device__ __forceinline__ void load4(const double *__restrict__ p, long long g, double (&v)[4])
+{
+    const double2 a = reinterpret_cast<const double2 *>(p)[2 * g], b = reinterpret_cast<const double2 *>(p)[2 * g + 1];
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+}
+
+// Adds the fluid nodes of group g (nodes 4g .. 4g+3) in node order.
+template <class R>
+__device__ __forceinline__ void mass_group(MassAcc<R> &acc, const uint8_t *__restrict__ type,
+                                           const R *__restrict__ rho, const R *__restrict__ mv, long long n,
+                                           long long g, int vec)
+{
+    const uchar4 t4 = reinterpret_cast<const uchar4 *>(type)[g];
+    const uint8_t t[4] = {t4.x, t4.y, t4.z, t4.w};
+    R d[4];
+    load4(rho, g, d);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (t[k] == FLUID) acc.add(d[k]);
+    if (mv) {
+        R a[4], b[4], c[4];
+        if (vec & 2) {
+            load4(mv, g, a);
+            load4(mv + n, g, b);
+            load4(mv + 2 * n, g, c);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) a[k] = mv[4 * g + k], b[k] = mv[n + 4 * g + k], c[k] = mv[2 * n + 4 * g + k];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (t[k] == FLUID) acc.speed(a[k], b[k], c[k]);
+    }
+}
+
+// Per-block partial (sum of rho, max |MV|^2, non-finite flag) over the fluid
+// nodes.  With vec bit 0 set (n a multiple of 4, type 4-byte and rho 16-byte
+// aligned) each thread takes groups of four nodes -- one 4-byte type load and
+// 16-byte field loads -- two groups per loop trip, both loaded before either
+// is added, so that every warp keeps two groups of loads in flight; bit 1
+// says MV is 16-byte aligned too.  The order in which a thread adds its
+// nodes does not depend on MV, so the mass is the same with or without it.
+// FP32 fields: at most 40 registers, so that the 6 blocks per SM of a large
+// box are resident together (FP64 fields: 48, 5 blocks).
+template <class R>
+__global__ void __launch_bounds__(kRedThreads, sizeof(R) == 4 ? kRedBlocks / 152 : 5) k_mass_partial(const uint8_t *__restrict__ type,
                                                              const R *__restrict__ rho,
-                                                             const R *__restrict__ mv, long long n,
+                                                             const R *__restrict__ mv, long long n, int vec,
                                                              double *__restrict__ part)
 {
-    double s = 0.0, mx = 0.0;
-    int bad = 0;
-    if (sizeof(R) == 4) {
-        // FP32 fields: each thread keeps its running sum as an exact FP32
-        // pair (TwoSum: hi + lo equals the sum of the values it added up to
-        // the rounding of lo), so the FP64 pipe -- a small fraction of the
-        // FP32 rate on this part -- only joins the threads' partials; the
-        // sign test and |MV|^2 stay in FP32 as the fields are
-        float hi = 0.f, lo = 0.f, m2 = 0.f;
-        for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
-             I += (long long)gridDim.x * blockDim.x) {
-            if (type[I] != FLUID) continue;
-            const float d = (float)rho[I];
-            if (!(d >= 0.f)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
-            const float t = hi + d, bp = t - hi;
-            lo += (hi - (t - bp)) + (d - bp);
-            hi = t;
-            if (mv) {
-                const float a = (float)mv[I], b = (float)mv[I + n], c = (float)mv[I + 2 * n];
-                m2 = fmaxf(m2, fmaf(a, a, fmaf(b, b, c * c)));
-            }
+    MassAcc<R> acc;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long first = 0;  // first node of the scalar loop
+    if (vec & 1) {
+        const long long ng = n >> 2;
+        first = ng << 2;
+        long long g = tid;
+        for (; g + stride < ng; g += 2 * stride) {
+            mass_group(acc, type, rho, mv, n, g, vec);
+            mass_group(acc, type, rho, mv, n, g + stride, vec);
         }
-        s = (double)hi + (double)lo;
-        mx = (double)m2;
-    } else {
-        for (long long I = (long long)blockIdx.x * blockDim.x + threadIdx.x; I < n;
-             I += (long long)gridDim.x * blockDim.x) {
-            if (type[I] != FLUID) continue;
-            const double d = (double)rho[I];
-            if (!(d >= 0.0)) bad = 1;  // NaN or negative (FluidCuda.cu:1632)
-            s += d;
-            if (mv) {
-                const double a = mv[I], b = mv[I + n], c = mv[I + 2 * n];
-                mx = fmax(mx, a * a + b * b + c * c);
-            }
-        }
+        if (g < ng) mass_group(acc, type, rho, mv, n, g, vec);
     }
+    for (long long I = first + tid; I < n; I += stride) {
+        if (type[I] != FLUID) continue;
+        acc.add(rho[I]);
+        if (mv) acc.speed(mv[I], mv[I + n], mv[I + 2 * n]);
+    }
+    double s = acc.sum(), mx = acc.max2();
+    int bad = acc.bad;
     __shared__ double ss[kRedThreads / 32], sm[kRedThreads / 32];
     __shared__ int sb[kRedThreads / 32];
     s = warp_sum(s);
@@ -243,7 +326,7 @@ void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long 
                       double *out, cudaStream_t st)
 {
     const int nb = diag_partial_blocks(n);
-    k_mass_partial<R><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, partials);
+    k_mass_partial<R><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, mass_vec_flags(type, rho, mv, n), partials);
     k_mass_final<<<1, kRedThreads, 0, st>>>(partials, nb, out, 0);
 }
 
@@ -491,7 +574,7 @@ extern "C" cpmp_status cpmp_mass_noalloc(const uint8_t *type, const float *rho, 
         return CPMP_ERR_CUDA;
     }
     const int nb = diag_partial_blocks(n);  // <= the array's kMaxRedBlocks triples
-    k_mass_partial<float><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, part);
+    k_mass_partial<float><<<nb, kRedThreads, 0, st>>>(type, rho, mv, n, mass_vec_flags(type, rho, mv, n), part);
     k_mass_final<<<1, kRedThreads, 0, st>>>(part, nb, out, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) {

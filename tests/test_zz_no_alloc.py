@@ -35,7 +35,8 @@ def _call(lib, typ, rho, mv, n, out, torch):
     return out.cpu().tolist()
 
 
-@pytest.mark.parametrize("dims", [(40, 16, 28), (70, 64, 61)], ids=["whole_blocks", "ragged_multipass"])
+@pytest.mark.parametrize("dims", [(40, 16, 28), (70, 64, 61), (67, 45, 93), (128, 128, 120)],
+                         ids=["whole_blocks", "ragged", "odd_n_scalar_multipass", "vector_two_group_trips"])
 def test_noalloc_reduction_matches_cpmp_reduce(cpmp, dims):
     torch = pytest.importorskip("torch")
     lib = cpmp.lib()
@@ -43,8 +44,15 @@ def test_noalloc_reduction_matches_cpmp_reduce(cpmp, dims):
     s = cpmp.Solver(dx=dx, dy=dy, dz=dz, scheme=cpmp.SCHEME["plain"], storage=cpmp.STORE["f32"],
                     base_pt=-0.04)
     s.set_flow_field(radius=min(dims) / 4.0, width=4.0)
-    if dims == (70, 64, 61):  # a partial last block and several nodes per thread
-        assert s.n % 256 != 0 and s.n > 1024 * 256
+    # the reduction grid has at most 912 blocks of 256 threads; n divisible by
+    # 4 takes groups of four nodes, two groups per loop trip where there are
+    # more than 2 x 912 x 256 groups, and any other n one node per trip
+    if dims == (70, 64, 61):  # a partial last block
+        assert s.n % 256 != 0 and s.n % 4 == 0
+    if dims == (67, 45, 93):  # the scalar loop, several nodes per thread
+        assert s.n % 4 != 0 and s.n > 912 * 256
+    if dims == (128, 128, 120):  # the group loop with two groups per trip and a remainder
+        assert s.n // 4 > 2 * 912 * 256
     out = torch.zeros(3, dtype=torch.float64, device="cuda")
     for call, steps in enumerate((5, 40)):
         s.step(steps)
