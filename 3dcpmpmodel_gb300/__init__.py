@@ -293,6 +293,15 @@ class Batch:
     def sync(self):
         _abi.check(self._lib.cpmp_batch_sync(self._b))
 
+    def reduce(self, allow_nonfinite: bool = False) -> list:
+        """Solver.reduce of every box, in four launches for the whole batch
+        (the same values, bit for bit)."""
+        arr = (Diag * len(self.boxes))()
+        rc = self._lib.cpmp_batch_reduce(self._b, arr, len(self.boxes))
+        if rc != 0 and not (allow_nonfinite and rc == _abi.CPMP_ERR_NONFINITE):
+            _abi.check(rc)
+        return [{k: getattr(d, k) for k, _ in Diag._fields_} for d in arr]
+
     def set_tile(self, tile_y: int, tile_z: int, march_x: int, nodes_per_thread: int = 1):
         _abi.check(self._lib.cpmp_batch_set_tile_ex(self._b, int(tile_y), int(tile_z), int(march_x),
                                                     int(nodes_per_thread)))

@@ -107,6 +107,7 @@ SIGNATURES = {
     "cpmp_batch_nodes": (C.c_longlong, [C.c_void_p]),
     "cpmp_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
     "cpmp_batch_sync": (C.c_int, [C.c_void_p]),
+    "cpmp_batch_reduce": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "cpmp_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "cpmp_batch_set_tile_ex": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "cpmp_batch_get_tile": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 4),

@@ -84,7 +84,9 @@ struct cpmp_batch {
     BatchBox *d_boxes = nullptr;
     unsigned *d_counter = nullptr;
     unsigned *d_mvmax = nullptr;  // [2][boxes]: each box's max |MV|^2 of its last collision, per parity
-    long long total_items = 0, nodes = 0, wall_blocks = 0, density_blocks = 0, launches = 0;
+    DiagBox *d_diag = nullptr;    // [boxes]: the batched diagnostics' box table
+    double *d_dout = nullptr;     // [boxes][kDiagStride]: their results
+    long long total_items = 0, nodes = 0, wall_blocks = 0, density_blocks = 0, mass_blocks = 0, launches = 0;
     cudaGraphExec_t gexec = nullptr;
     std::unique_ptr<LaunchHook> hook;
     bool timing = false;
@@ -734,6 +736,34 @@ cpmp_status cpmp_set_field(cpmp_handle *h, cpmp_field f, int dtype, const void *
     return CPMP_OK;
 }
 
+// A box's diagnostics from its kDiagStride result doubles and, for the FUSED
+// scheme, the max |MV|^2 bits its last collision left.
+static void diag_fill(const cpmp_handle *h, const double *r, unsigned mvbits, cpmp_diag *out)
+{
+    double m2 = r[1];
+    if (!h->plain) {
+        float f;
+        std::memcpy(&f, &mvbits, sizeof(f));
+        m2 = std::max(m2, (double)f);
+    }
+    out->mass = r[0];
+    out->max_speed = std::sqrt(m2);
+    out->nonfinite = r[2] != 0.0;
+    if (h->p.dx >= 8 && h->p.dz >= 8) {
+        out->ca_left = r[4];
+        out->ca_right = r[5];
+        out->ca_cap = r[6];
+        out->x_left = r[7];
+        out->x_right = r[8];
+        out->cap_h = r[9];
+        out->cap_l = r[10];
+    }
+    out->lap_r = r[12];
+    out->lap_dp = r[13];
+    out->lap_sigma = r[14];
+    out->step = h->step;
+}
+
 cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
 {
     if (!h || !out) return fail(CPMP_ERR_PARAM, "null argument");
@@ -761,35 +791,15 @@ cpmp_status cpmp_reduce(cpmp_handle *h, cpmp_diag *out)
                                    h->p.k * h->p.k, h->dout + 12, h->st);
     }
     h->launches += 4;
-    double r[16] = {0};
+    double r[kDiagStride] = {0};
     unsigned mvbits = 0;
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(r, h->dout, 16 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(r, h->dout, kDiagStride * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     if (h->sdiag && h->step > 0)
         CK(cudaMemcpyAsync(&mvbits, h->sdiag + ((h->step - 1) & 1) * h->sdiag_stride, sizeof(unsigned),
                            cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    if (!h->plain) {
-        float m2;
-        std::memcpy(&m2, &mvbits, sizeof(m2));
-        r[1] = std::max(r[1], (double)m2);
-    }
-    out->mass = r[0];
-    out->max_speed = std::sqrt(r[1]);
-    out->nonfinite = r[2] != 0.0;
-    if (h->p.dx >= 8 && h->p.dz >= 8) {
-        out->ca_left = r[4];
-        out->ca_right = r[5];
-        out->ca_cap = r[6];
-        out->x_left = r[7];
-        out->x_right = r[8];
-        out->cap_h = r[9];
-        out->cap_l = r[10];
-    }
-    out->lap_r = r[12];
-    out->lap_dp = r[13];
-    out->lap_sigma = r[14];
-    out->step = h->step;
+    diag_fill(h, r, mvbits, out);
     if (out->nonfinite) return fail(CPMP_ERR_NONFINITE, "NaN or negative density on a fluid node");
     return CPMP_OK;
 }
@@ -1069,8 +1079,37 @@ cpmp_status batch_upload(cpmp_batch *b)
     b->total_items = item;
     b->wall_blocks = wblk;
     b->density_blocks = dblk;
+    // the batched diagnostics: each box's mass blocks follow the previous box's
+    std::vector<DiagBox> dg(nb);
+    long long mblk = 0;
+    for (int i = 0; i < nb; ++i) {
+        const cpmp_handle *h = b->boxes[i];
+        DiagBox &d = dg[i];
+        d.type = h->type;
+        d.rho[0] = bx[i].rho[0];
+        d.rho[1] = bx[i].rho[1];
+        d.part = h->partials;
+        d.n = h->n;
+        d.blk0 = mblk;
+        d.nb = diag_partial_blocks(h->n);
+        d.vec = diag_mass_vec_flags(h->type, d.rho[0], nullptr, h->n) & diag_mass_vec_flags(h->type, d.rho[1], nullptr, h->n);
+        mblk += d.nb;
+        d.dx = h->p.dx;
+        d.dy = h->p.dy;
+        d.dz = h->p.dz;
+        d.tier = h->p.dy / 2;
+        d.angle = (h->p.dx >= 8 && h->p.dz >= 8) ? 1 : 0;
+        d.eos = h->eos;
+        d.mid = (h->den_g + h->den_l) / 2;
+        d.A = h->A;
+        d.B = h->B;
+        d.T = h->T;
+        d.kk = h->p.k * h->p.k;
+    }
+    b->mass_blocks = mblk;
     CK(cudaMemcpyAsync(b->d_params, kp.data(), nb * sizeof(KParams<float>), cudaMemcpyHostToDevice, b->st));
     CK(cudaMemcpyAsync(b->d_boxes, bx.data(), nb * sizeof(BatchBox), cudaMemcpyHostToDevice, b->st));
+    CK(cudaMemcpyAsync(b->d_diag, dg.data(), nb * sizeof(DiagBox), cudaMemcpyHostToDevice, b->st));
     CK(cudaStreamSynchronize(b->st));
     return CPMP_OK;
 }
@@ -1133,6 +1172,8 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
         if (b->d_boxes) cudaFree(b->d_boxes);
         if (b->d_counter) cudaFree(b->d_counter);
         if (b->d_mvmax) cudaFree(b->d_mvmax);
+        if (b->d_diag) cudaFree(b->d_diag);
+        if (b->d_dout) cudaFree(b->d_dout);
         cudaStreamDestroy(b->st);
     };
     for (int i = 0; i < count; ++i) {
@@ -1157,7 +1198,10 @@ cpmp_status cpmp_batch_create(const cpmp_params *params, int count, cpmp_batch *
     if ((s = dalloc((void **)&b->d_params, count * sizeof(KParams<float>), "batch params")) != CPMP_OK ||
         (s = dalloc((void **)&b->d_boxes, count * sizeof(BatchBox), "batch boxes")) != CPMP_OK ||
         (s = dalloc((void **)&b->d_counter, sizeof(unsigned), "batch counter")) != CPMP_OK ||
-        (s = dalloc((void **)&b->d_mvmax, 2 * count * sizeof(unsigned), "batch mv max")) != CPMP_OK) {
+        (s = dalloc((void **)&b->d_mvmax, 2 * count * sizeof(unsigned), "batch mv max")) != CPMP_OK ||
+        (s = dalloc((void **)&b->d_diag, count * sizeof(DiagBox), "batch diagnostics table")) != CPMP_OK ||
+        (s = dalloc((void **)&b->d_dout, (size_t)count * kDiagStride * sizeof(double), "batch diagnostics")) !=
+            CPMP_OK) {
         cleanup();
         return s;
     }
@@ -1248,6 +1292,36 @@ cpmp_status cpmp_batch_sync(cpmp_batch *b)
     if (!b) return fail(CPMP_ERR_PARAM, "null batch");
     CK(cudaSetDevice(b->device));
     CK(cudaStreamSynchronize(b->st));
+    return CPMP_OK;
+}
+
+cpmp_status cpmp_batch_reduce(cpmp_batch *b, cpmp_diag *out, int count)
+{
+    if (!b || !out) return fail(CPMP_ERR_PARAM, "null argument");
+    const int nb = (int)b->boxes.size();
+    if (count != nb) return fail(CPMP_ERR_PARAM, "out must hold one cpmp_diag per box of the batch");
+    cpmp_status s;
+    if ((s = batch_check(b)) != CPMP_OK) return s;
+    CK(cudaSetDevice(b->device));
+    std::memset(out, 0, (size_t)nb * sizeof(cpmp_diag));
+    const long long step = b->boxes[0]->step;
+    diag_launch_batch(b->d_diag, nb, b->mass_blocks, (int)(step & 1), b->d_dout, b->st);
+    b->launches += 4;
+    std::vector<double> r((size_t)nb * kDiagStride);
+    std::vector<unsigned> mv(nb, 0u);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(r.data(), b->d_dout, r.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    if (step > 0)
+        CK(cudaMemcpyAsync(mv.data(), b->d_mvmax + ((step - 1) & 1) * nb, nb * sizeof(unsigned),
+                           cudaMemcpyDeviceToHost, b->st));
+    CK(cudaStreamSynchronize(b->st));
+    int bad = -1;
+    for (int i = 0; i < nb; ++i) {
+        diag_fill(b->boxes[i], r.data() + (size_t)i * kDiagStride, mv[i], out + i);
+        if (out[i].nonfinite && bad < 0) bad = i;
+    }
+    if (bad >= 0)
+        return fail(CPMP_ERR_NONFINITE, "NaN or negative density on a fluid node of box " + std::to_string(bad));
     return CPMP_OK;
 }
 
@@ -1434,6 +1508,8 @@ void cpmp_batch_destroy(cpmp_batch *b)
     cudaFree(b->d_boxes);
     cudaFree(b->d_counter);
     cudaFree(b->d_mvmax);
+    cudaFree(b->d_diag);
+    cudaFree(b->d_dout);
     cudaStreamDestroy(b->st);
     b->hook.reset();
     delete b;

@@ -154,17 +154,14 @@ __device__ __forceinline__ void mass_group(MassAcc<R> &acc, const uint8_t *__res
 // is added, so that every warp keeps two groups of loads in flight; bit 1
 // says MV is 16-byte aligned too.  The order in which a thread adds its
 // nodes does not depend on MV, so the mass is the same with or without it.
-// FP32 fields: at most 40 registers, so that the 6 blocks per SM of a large
-// box are resident together (FP64 fields: 48, 5 blocks).
+// One block of the pass: thread tid of `stride` threads; the block's triple
+// goes to part[0..2].
 template <class R>
-__global__ void __launch_bounds__(kRedThreads, sizeof(R) == 4 ? kRedBlocks / 152 : 5) k_mass_partial(const uint8_t *__restrict__ type,
-                                                             const R *__restrict__ rho,
-                                                             const R *__restrict__ mv, long long n, int vec,
-                                                             double *__restrict__ part)
+__device__ __forceinline__ void mass_partial_block(const uint8_t *__restrict__ type, const R *__restrict__ rho,
+                                                   const R *__restrict__ mv, long long n, int vec, long long tid,
+                                                   long long stride, double *__restrict__ part)
 {
     MassAcc<R> acc;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     long long first = 0;  // first node of the scalar loop
     if (vec & 1) {
         const long long ng = n >> 2;
@@ -203,14 +200,26 @@ __global__ void __launch_bounds__(kRedThreads, sizeof(R) == 4 ? kRedBlocks / 152
             tm = fmax(tm, sm[k]);
             tb |= sb[k];
         }
-        part[3 * blockIdx.x] = ts;
-        part[3 * blockIdx.x + 1] = tm;
-        part[3 * blockIdx.x + 2] = (double)tb;
+        part[0] = ts;
+        part[1] = tm;
+        part[2] = (double)tb;
     }
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__restrict__ part, int nb,
-                                                           double *__restrict__ out, int take_sqrt)
+// FP32 fields: at most 40 registers, so that the 6 blocks per SM of a large
+// box are resident together (FP64 fields: 64, 4 blocks).
+template <class R>
+__global__ void __launch_bounds__(kRedThreads, sizeof(R) == 4 ? kRedBlocks / 152 : 4)
+    k_mass_partial(const uint8_t *__restrict__ type, const R *__restrict__ rho, const R *__restrict__ mv,
+                   long long n, int vec, double *__restrict__ part)
+{
+    mass_partial_block<R>(type, rho, mv, n, vec, (long long)blockIdx.x * kRedThreads + threadIdx.x,
+                          (long long)gridDim.x * kRedThreads, part + 3 * blockIdx.x);
+}
+
+// Joins nb partial triples (one block of kRedThreads threads).
+__device__ __forceinline__ void mass_final_block(const double *__restrict__ part, int nb, double *__restrict__ out,
+                                                 int take_sqrt)
 {
     __shared__ double ss[kRedThreads], sm[kRedThreads], sb[kRedThreads];
     double s = 0.0, mx = 0.0, b = 0.0;
@@ -236,6 +245,12 @@ __global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__rest
         out[1] = take_sqrt ? sqrt(sm[0]) : sm[0];
         out[2] = sb[0];
     }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mass_final(const double *__restrict__ part, int nb,
+                                                           double *__restrict__ out, int take_sqrt)
+{
+    mass_final_block(part, nb, out, take_sqrt);
 }
 
 // ------------------------------------------------ droplet-impact sums ----
@@ -339,8 +354,8 @@ void diag_launch_mass(const uint8_t *type, const R *rho, const R *mv, long long 
 // keeps the last hit, the maximum k).  Thread 0 does the extrapolation and
 // angle arithmetic in FP64 exactly as the reference.
 template <class R>
-__global__ void k_contact_angle(const R *__restrict__ rho, int dx, int dy, int dz, int tier,
-                                double mid, double *__restrict__ out)
+__device__ __forceinline__ void contact_angle_block(const R *__restrict__ rho, int dx, int dy, int dz, int tier,
+                                                    double mid, double *__restrict__ out)
 {
     __shared__ double px[8];
     __shared__ int ic_s;
@@ -446,6 +461,13 @@ __global__ void k_contact_angle(const R *__restrict__ rho, int dx, int dy, int d
 }
 
 template <class R>
+__global__ void __launch_bounds__(288) k_contact_angle(const R *__restrict__ rho, int dx, int dy, int dz, int tier,
+                                                       double mid, double *__restrict__ out)
+{
+    contact_angle_block<R>(rho, dx, dy, dz, tier, mid, out);
+}
+
+template <class R>
 void diag_launch_contact_angle(const R *rho, int dx, int dy, int dz, int tier, double den_g,
                                double den_l, double *out, cudaStream_t st)
 {
@@ -465,8 +487,8 @@ __device__ double eos_pressure(int eos, double A, double B, double T, double r)
 }
 
 template <class R>
-__global__ void k_laplace(const R *__restrict__ rho, int dx, int dy, int dz, int eos, double A,
-                          double B, double T, double kk, double *__restrict__ out)
+__device__ __forceinline__ void laplace_warp(const R *__restrict__ rho, int dx, int dy, int dz, int eos, double A,
+                                             double B, double T, double kk, double *__restrict__ out)
 {
     const int l = threadIdx.x;
     auto D = [&](int j) -> double { return (double)rho[((long long)(dx / 2) * dy + j) * dz + dz / 2]; };
@@ -492,10 +514,77 @@ __global__ void k_laplace(const R *__restrict__ rho, int dx, int dy, int dz, int
 }
 
 template <class R>
+__global__ void k_laplace(const R *__restrict__ rho, int dx, int dy, int dz, int eos, double A, double B, double T,
+                          double kk, double *__restrict__ out)
+{
+    laplace_warp<R>(rho, dx, dy, dz, eos, A, B, T, kk, out);
+}
+
+template <class R>
 void diag_launch_laplace(const R *rho, int dx, int dy, int dz, int eos, double A, double B, double T,
                          double kk, double *out, cudaStream_t st)
 {
     k_laplace<R><<<1, 32, 0, st>>>(rho, dx, dy, dz, eos, A, B, T, kk, out);
+}
+
+// ------------------------------------------------ batched diagnostics ----
+// The diagnostics of every box of a batch in four launches: the mass pass
+// over a flattened grid (box b owns mass blocks blk0 .. blk0 + nb - 1, and
+// each of them does what block (local index) of the box's own mass pass
+// does, over the same threads and nodes), then one block per box for the
+// join, the contact angle and the Laplace probe.  Every box's results are
+// those of its own reduction, bit for bit.
+__global__ void __launch_bounds__(kRedThreads, kRedBlocks / 152)
+    k_mass_partial_batch(const DiagBox *__restrict__ boxes, int nbox, int par)
+{
+    const long long g = blockIdx.x;
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {  // the last box whose first block is at most g
+        const int mid = (lo + hi + 1) >> 1;
+        if (boxes[mid].blk0 <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const DiagBox &d = boxes[lo];
+    const long long local = g - d.blk0;
+    mass_partial_block<float>(d.type, d.rho[par], nullptr, d.n, d.vec, local * kRedThreads + threadIdx.x,
+                              (long long)d.nb * kRedThreads, d.part + 3 * local);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mass_final_batch(const DiagBox *__restrict__ boxes,
+                                                                 double *__restrict__ out)
+{
+    const DiagBox &d = boxes[blockIdx.x];
+    mass_final_block(d.part, d.nb, out + kDiagStride * blockIdx.x, 0);
+}
+
+__global__ void __launch_bounds__(288) k_contact_angle_batch(const DiagBox *__restrict__ boxes, int par,
+                                                             double *__restrict__ out)
+{
+    const DiagBox &d = boxes[blockIdx.x];
+    if (!d.angle) return;  // the whole block: a box too small for the slice search
+    contact_angle_block<float>(d.rho[par], d.dx, d.dy, d.dz, d.tier, d.mid, out + kDiagStride * blockIdx.x + 4);
+}
+
+__global__ void __launch_bounds__(32) k_laplace_batch(const DiagBox *__restrict__ boxes, int par,
+                                                      double *__restrict__ out)
+{
+    const DiagBox &d = boxes[blockIdx.x];
+    laplace_warp<float>(d.rho[par], d.dx, d.dy, d.dz, d.eos, d.A, d.B, d.T, d.kk,
+                        out + kDiagStride * blockIdx.x + 12);
+}
+
+void diag_launch_batch(const DiagBox *boxes, int nbox, long long mass_blocks, int par, double *out,
+                       cudaStream_t st)
+{
+    k_mass_partial_batch<<<(unsigned)mass_blocks, kRedThreads, 0, st>>>(boxes, nbox, par);
+    k_mass_final_batch<<<nbox, kRedThreads, 0, st>>>(boxes, out);
+    k_contact_angle_batch<<<nbox, 288, 0, st>>>(boxes, par, out);
+    k_laplace_batch<<<nbox, 32, 0, st>>>(boxes, par, out);
+}
+
+int diag_mass_vec_flags(const void *type, const void *rho, const void *mv, long long n)
+{
+    return mass_vec_flags(type, rho, mv, n);
 }
 
 __global__ void k_mv(const uint8_t *type, const float *rho, const float *u, const float *F, float *mv,

@@ -54,17 +54,11 @@ __device__ __forceinline__ int wrap1(int a, int n) { return a < 0 ? a + n : (a >
 // The 18 moving-population arrays (slot k holds direction k + 1 of the A-A
 // addressing): as base pointers in the launch's parameter space, so that an
 // access is one multiply-add on a constant operand, in shared memory (the
-// items of a batch, whose boxes differ), or as h + n k.
+// items and the density blocks of a batch, whose boxes differ).
 template <class S>
 struct SlotTable {
     S *q[Q - 1];
     __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return q[k] + idx; }
-};
-template <class S>
-struct SlotBase {
-    S *h;
-    unsigned n;
-    __device__ __forceinline__ S *operator()(int k, unsigned idx) const { return h + (size_t)n * (unsigned)k + idx; }
 };
 template <class S>
 struct SlotShared {
@@ -212,8 +206,10 @@ __device__ __forceinline__ bool z_plain(const KParams<float> &p, int k)
 // paired FP32 (the sums of density_node).  With
 // an even DZ every pair of loads has a parity known at compile time (node
 // index and N even, so it is that of cz(q)) and aligned pairs are vector
-// loads; otherwise all moving-population and anchor loads are scalar.  Every
-// load is issued before the first add so their latencies overlap.
+// loads; otherwise all moving-population and anchor loads are scalar (vector
+// loads where a pair's address happens to be aligned, chosen at run time,
+// measured slower: the two load paths cost more than the loads they save).
+// Every load is issued before the first add so their latencies overlap.
 // botw / topw (even DZ only): the pair is (2, 3) / (dz-4, dz-3) of an x/y-
 // interior column of a walled box: its fluid node's sources across the wall
 // layer are its own slots and rest population (density_wall_node's sums, by
@@ -903,6 +899,11 @@ __global__ void __launch_bounds__(BATCH_DENSITY_BLOCK, 8) k_density_batch(const 
     const int b = batch_box_of(boxes, nbox, g, [](const BatchBox &x) { return x.dblk0; });
     const KParams<float> &p = params[b];
     const BatchBox &bx = boxes[b];
+    // a block's threads all belong to box b: its 18 slot pointers once per
+    // block, in shared memory (computed per thread they crowd the registers)
+    __shared__ const S *slot_s[Q - 1];
+    if (threadIdx.x < Q - 1) slot_s[threadIdx.x] = (const S *)bx.h + (size_t)p.n * threadIdx.x;
+    __syncthreads();
     const int ppc = pairs_per_column(p.dz);
     const int per_plane = (int)(((long long)p.dy * ppc + BATCH_DENSITY_BLOCK - 1) / BATCH_DENSITY_BLOCK);
     const long long local = g - bx.dblk0;
@@ -910,8 +911,8 @@ __global__ void __launch_bounds__(BATCH_DENSITY_BLOCK, 8) k_density_batch(const 
     const int e = (int)(local - (long long)i * per_plane) * BATCH_DENSITY_BLOCK + threadIdx.x;
     if (e >= p.dy * ppc) return;
     const int j = e / ppc, t = e - j * ppc;
-    density_pair<S>(p, P, (const S *)bx.h, SlotBase<const S>{(const S *)bx.h, (unsigned)p.n}, bx.f0[P], bx.rho[P], i,
-                    j, pair_k0(p, i, j, t));
+    density_pair<S>(p, P, (const S *)bx.h, SlotShared<const S>{slot_s}, bx.f0[P], bx.rho[P], i, j,
+                    pair_k0(p, i, j, t));
 }
 
 template <class S, int TY, int TZ, int L>

@@ -164,6 +164,27 @@ extern template void adj_launch_loss<double>(const KParams<double> &, const uint
 extern template void adj_launch_step<double>(const KParams<double> &, const uint8_t *, const double *, const double *, const double *, const double *, AdjBufs<double> &, cudaStream_t, LaunchHook *);
 
 // ---- diagnostics (k_diag.cu) ----------------------------------------------
+// Results of one box's diagnostics, kDiagStride doubles: [0] sum rho over the
+// fluid nodes, [1] max |MV|^2, [2] non-finite flag, [4..10] the contact angle
+// (CaLeft, CaRight, CaCap, XLeft, XRight, H, L), [12..14] the Laplace probe
+// (R, dp, sigma).
+constexpr int kDiagStride = 16;
+// One box of a batched diagnostics pass (FUSED boxes: FP32 density, no MV).
+struct DiagBox {
+    const uint8_t *type;
+    const float *rho[2];  // the density after an even / odd number of steps
+    double *part;         // the box's 3 * nb mass partials
+    long long n, blk0;    // nodes; the box's first block in the flattened mass grid
+    int nb, vec;          // diag_partial_blocks(n); diag_mass_vec_flags of type and both rho
+    int dx, dy, dz, tier, angle, eos;  // angle: dx >= 8 and dz >= 8 (the slice search runs)
+    double mid, A, B, T, kk;           // (den_g + den_l) / 2; EOS constants, K^2
+};
+// The diagnostics of nbox boxes: out[kDiagStride * b + ...] as above (the
+// max |MV|^2 slot stays 0); mass_blocks = sum of the boxes' nb; par = the
+// step count's parity, which selects rho[par].
+void diag_launch_batch(const DiagBox *boxes, int nbox, long long mass_blocks, int par, double *out,
+                       cudaStream_t st);
+int diag_mass_vec_flags(const void *type, const void *rho, const void *mv, long long n);
 // Deterministic FP64 reduction: out[0] = sum rho (fluid), out[1] = max |mv|^2,
 // out[2] = non-finite flag.  `partials` holds 3 * diag_partial_blocks(n)
 // doubles.

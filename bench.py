@@ -467,17 +467,16 @@ def run_batch(args, wl: dict, cp, torch) -> None:
             cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
                                              hf.ctypes.data_as(C.c_void_p), C.c_size_t(hf.nbytes)))
         torch.cuda.synchronize()
-        diag = cp.Diag()
+        diags = (cp.Diag * len(b.boxes))()
         t0 = time.perf_counter()
         for s, hf in zip(b.boxes, host_f):
             cp._abi.check(cpl.cpmp_set_field(s._h, cp.FIELD["dist"], cp._abi.CPMP_F32,
                                              hf.ctypes.data_as(C.c_void_p), C.c_size_t(hf.nbytes)))
         for _ in range(args.steps):
             b.step(1)
-            for s in b.boxes:
-                rc = cpl.cpmp_reduce(s._h, C.byref(diag))
-                if rc not in (0, cp._abi.CPMP_ERR_NONFINITE):
-                    cp._abi.check(rc)
+            rc = cpl.cpmp_batch_reduce(b._b, diags, len(b.boxes))
+            if rc not in (0, cp._abi.CPMP_ERR_NONFINITE):
+                cp._abi.check(rc)
         for s, hr in zip(b.boxes, host_r):
             cp._abi.check(cpl.cpmp_get_field(s._h, cp.FIELD["rho"], cp._abi.CPMP_F32,
                                              hr.ctypes.data_as(C.c_void_p), C.c_size_t(hr.nbytes)))
@@ -487,7 +486,7 @@ def run_batch(args, wl: dict, cp, torch) -> None:
                "d2h_bytes_per_step": int((sum(h.nbytes for h in host_r) + args.steps * len(b.boxes) *
                                           C.sizeof(cp.Diag)) / args.steps),
                "what": "cpmp_set_field(DIST, pinned FP32) of every box + K x (cpmp_batch_step(1) + "
-                       "cpmp_reduce of every box) + cpmp_get_field(RHO, pinned FP32) of every box"}
+                       "cpmp_batch_reduce: every box's diagnostics) + cpmp_get_field(RHO, pinned FP32) of every box"}
     cpu = None if args.no_cpu else cpu_sample(args, batch_sample_workload(wl))
     line = {
         "metric": metric_name(args) + " (aggregate over a batch)", "value": round(value, 1), "unit": "MLUPS",

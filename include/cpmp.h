@@ -313,10 +313,11 @@ cpmp_status cpmp_adjoint(cpmp_handle *h, int steps, int checkpoint_every, const 
  * No reference counterpart (the reference runs one box per process).  All
  * boxes use the FUSED scheme and share storage, lap_order, wall_mode,
  * complex_bc and device; grid, EOS model, T/Tc, K, kappa, rates and wall
- * potential may differ per box.  Each time step is three batched wall
- * passes, ONE persistent fused-collide launch whose CTAs take (box, tile,
- * x-chunk) work items from a device counter until none are left, and one
- * batched density pass; cpmp_batch_step replays two steps as a CUDA graph. */
+ * potential may differ per box.  Each time step is one batched wall pass
+ * (the three wall layers of every box), ONE persistent fused-collide launch
+ * whose CTAs take (box, tile, x-chunk) work items from a device counter until
+ * none are left, and one batched density pass; cpmp_batch_step replays two
+ * steps as a CUDA graph. */
 typedef struct cpmp_batch cpmp_batch;
 
 /* Creates count boxes from params[count] (every box an ordinary handle that
@@ -332,6 +333,12 @@ long long cpmp_batch_nodes(cpmp_batch *b);   /* total lattice nodes of all boxes
 /* nsteps time steps of every box (asynchronous on the batch stream). */
 cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps);
 cpmp_status cpmp_batch_sync(cpmp_batch *b);
+/* cpmp_reduce of every box (out[count], count = the number of boxes), in
+ * four launches for the whole batch and one wait: each out[i] equals what
+ * cpmp_reduce on box i returns, bit for bit.  Returns CPMP_ERR_NONFINITE (with
+ * every out[i] filled) when any box has a NaN or negative fluid density; the
+ * error message names the first such box. */
+cpmp_status cpmp_batch_reduce(cpmp_batch *b, cpmp_diag *out, int count);
 /* Tile shape / x-march shared by all boxes; the autotuner times the
  * candidates on scratch copies of every box (the state is not advanced). */
 cpmp_status cpmp_batch_set_tile(cpmp_batch *b, int tile_y, int tile_z, int march_x);

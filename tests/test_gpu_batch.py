@@ -73,3 +73,29 @@ def test_batch_autotune_keeps_the_state(cpmp):
         assert s.reduce()["max_speed"] == v  # the scratch steps leave the diagnostics alone
     b.step(2)
     b.close()
+
+
+def test_batch_reduce_equals_each_box_reduce(cpmp):
+    """cpmp_batch_reduce (four launches for all boxes) returns each box's
+    cpmp_reduce bit for bit: boxes whose node count is a multiple of 4 or not,
+    one too small for the contact-angle slice (dx < 8), one larger than the
+    mass pass's 912 x 256 threads."""
+    boxes = BOXES + [
+        dict(dx=33, dy=17, dz=27, model=202, tr=0.7, base_pt=0.02, radius=7.0),  # N odd
+        dict(dx=6, dy=12, dz=20, model=201, tr=0.8, base_pt=0.0, radius=4.0),    # no contact angle
+        dict(dx=96, dy=64, dz=44, model=202, tr=0.75, base_pt=-0.04, radius=16.0),
+    ]
+    b = cpmp.Batch([params_of(cpmp, box, "f16") for box in boxes])
+    for s, box in zip(b.boxes, boxes):
+        s.set_flow_field(radius=box["radius"], width=4.0)
+    assert b.boxes[-1].n > 912 * 256 and b.boxes[3].n % 4 != 0
+    done = 0
+    for steps in (0, 5, 2):  # before any step, then odd and even step counts
+        b.step(steps)
+        done += steps
+        got = b.reduce()
+        for s, g in zip(b.boxes, got):
+            assert g == s.reduce()
+        assert got[0]["step"] == done
+    assert got[0]["max_speed"] > 0 and got[5]["mass"] > 0
+    b.close()
