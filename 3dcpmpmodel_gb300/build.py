@@ -36,6 +36,9 @@ UNITS = [
     ("k_split_f16.cu", ["--fmad=false"]),
     ("k_split_bf16.cu", ["--fmad=false"]),
     ("k_split_f32.cu", ["--fmad=false"]),
+    ("k_batch_f16.cu", ["--fmad=false"]),
+    ("k_batch_bf16.cu", ["--fmad=false"]),
+    ("k_batch_f32.cu", ["--fmad=false"]),
     # no FMA contraction: the reductions give the same bits whether a single
     # box's kernel or the batched one runs them
     ("k_diag.cu", ["--fmad=false"]),

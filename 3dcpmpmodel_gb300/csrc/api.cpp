@@ -87,6 +87,7 @@ struct cpmp_batch {
     DiagBox *d_diag = nullptr;    // [boxes]: the batched diagnostics' box table
     double *d_dout = nullptr;     // [boxes][kDiagStride]: their results
     long long total_items = 0, nodes = 0, wall_blocks = 0, density_blocks = 0, mass_blocks = 0, launches = 0;
+    bool ref_rates = false;       // every box's rates follow the reference's pattern
     cudaGraphExec_t gexec = nullptr;
     std::unique_ptr<LaunchHook> hook;
     bool timing = false;
@@ -1079,6 +1080,7 @@ cpmp_status batch_upload(cpmp_batch *b)
     b->total_items = item;
     b->wall_blocks = wblk;
     b->density_blocks = dblk;
+    b->ref_rates = std::all_of(kp.begin(), kp.end(), [](const KParams<float> &k) { return reference_rates(k); });
     // the batched diagnostics: each box's mass blocks follow the previous box's
     std::vector<DiagBox> dg(nb);
     long long mblk = 0;
@@ -1120,7 +1122,8 @@ void batch_one_step(cpmp_batch *b, LaunchHook *hook, bool bookkeeping)
     const size_t nb = b->boxes.size();
     cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
     fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params, b->d_boxes,
-                     (int)b->boxes.size(), b->total_items, b->wall_blocks, b->density_blocks, P, b->d_counter, b->st, hook);
+                     (int)b->boxes.size(), b->total_items, b->wall_blocks, b->density_blocks, P, b->d_counter,
+                     b->ref_rates, b->st, hook);
     if (!bookkeeping) return;
     for (cpmp_handle *h : b->boxes) {
         h->step += 1;
@@ -1264,7 +1267,7 @@ cpmp_status cpmp_batch_step(cpmp_batch *b, int nsteps)
                 cudaMemsetAsync(b->d_mvmax + P * nb, 0, nb * sizeof(unsigned), b->st);
                 fused_batch_step(b->storage, b->lap_order, b->wall_mode, b->complex_bc, b->tile, b->d_params,
                                  b->d_boxes, (int)b->boxes.size(), b->total_items, b->wall_blocks, b->density_blocks, P,
-                                 b->d_counter, b->st, nullptr);
+                                 b->d_counter, b->ref_rates, b->st, nullptr);
             }
             cudaError_t e = cudaStreamEndCapture(b->st, &g);
             if (e != cudaSuccess) return fail(CPMP_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));

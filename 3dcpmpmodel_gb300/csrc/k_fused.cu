@@ -225,10 +225,13 @@ void set_attr_t(int si, int max_smem)
     bool ok = (int)b <= max_smem;
     if (ok)
         ok = cudaFuncSetAttribute(k_fused_collide<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)b) == cudaSuccess &&
-             cudaFuncSetAttribute(k_fused_collide_batch<S, TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)b) == cudaSuccess;
     cudaGetLastError();
+    // the batches' collide of the same tile (its own unit per storage)
+    if (ok)
+        ok = si == 0   ? batch_set_attr_f16(L == 3 ? 7 : 5, TY, TZ, max_smem)
+             : si == 1 ? batch_set_attr_bf16(L == 3 ? 7 : 5, TY, TZ, max_smem)
+                       : batch_set_attr_f32(L == 3 ? 7 : 5, TY, TZ, max_smem);
     g_usable[si][L - 2][tile_index(TY, TZ)] = ok;
 }
 template <class S, int L>
@@ -355,37 +358,10 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 }
 
 // ------------------------------------------------------------- batches ----
-namespace {
-template <class S, int TY, int TZ, int L>
-void batch_collide_t(const KParams<float> *params, const BatchBox *boxes, int nbox, long long total, int P,
-                     int xl, unsigned *counter, cudaStream_t st)
-{
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_collide_batch<S, TY, TZ, L>, TY * TZ,
-                                                  fused_smem_bytes<S, TY, TZ, L>());
-    long long grid = (long long)sms * std::max(per_sm, 1);
-    if (grid > total) grid = total;
-    if (grid < 1) grid = 1;
-    k_fused_collide_batch<S, TY, TZ, L><<<(unsigned)grid, TY * TZ, fused_smem_bytes<S, TY, TZ, L>(), st>>>(
-        params, boxes, nbox, total, P, xl, counter);
-}
-template <class S, int L>
-void batch_collide_l(const FusedTile &t, const KParams<float> *params, const BatchBox *boxes, int nbox,
-                     long long total, int P, unsigned *counter, cudaStream_t st)
-{
-    if (t.ty == 4 && t.tz == 32) batch_collide_t<S, 4, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else if (t.ty == 8 && t.tz == 32) batch_collide_t<S, 8, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else if (t.ty == 16 && t.tz == 32) batch_collide_t<S, 16, 32, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else if (t.ty == 16 && t.tz == 16) batch_collide_t<S, 16, 16, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-    else batch_collide_t<S, 8, 16, L>(params, boxes, nbox, total, P, t.xl, counter, st);
-}
-}  // namespace
 
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      long long wall_blocks, long long density_blocks, int P, unsigned *counter,
+                      long long wall_blocks, long long density_blocks, int P, unsigned *counter, bool ref_rates,
                       cudaStream_t st, LaunchHook *hook)
 {
     if (wall_mode == 1 && wall_blocks > 0) {
@@ -395,13 +371,12 @@ void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc,
     }
     hook_begin(hook, K_FUSED, st);
     cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-    with_storage(storage, [&](auto tag) {
-        using S = decltype(tag);
-        if (lap_order == 7)
-            batch_collide_l<S, 3>(t, params, boxes, nbox, total_items, P, counter, st);
-        else
-            batch_collide_l<S, 2>(t, params, boxes, nbox, total_items, P, counter, st);
-    });
+    if (storage == CPMP_STORE_F16)
+        batch_collide_launch_f16(lap_order, t, params, boxes, nbox, total_items, P, counter, ref_rates, st);
+    else if (storage == CPMP_STORE_BF16)
+        batch_collide_launch_bf16(lap_order, t, params, boxes, nbox, total_items, P, counter, ref_rates, st);
+    else
+        batch_collide_launch_f32(lap_order, t, params, boxes, nbox, total_items, P, counter, ref_rates, st);
     hook_end(hook, K_FUSED, st);
     hook_begin(hook, K_DENSITY, st);
     with_storage(storage, [&](auto tag) {

@@ -662,7 +662,8 @@ __device__ __forceinline__ void mvmax_flush(const KParams<float> &p, int P, floa
 template <int TY, int TZ, int L>
 using Rings1 = FusedRings<TY, TZ, L, TY * TZ, 1>;
 
-template <class S, int TY, int TZ, int L, class SL>
+// REF: the rates follow the reference's pattern (collide36's compile-time case).
+template <class S, int TY, int TZ, int L, bool REF = false, class SL>
 __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const SL &slots,
                                            const float *__restrict__ f0c, float *__restrict__ f0n,
                                            const float *__restrict__ rho, const int z0, const int y0,
@@ -774,9 +775,9 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             if (p.qp) {
                 float qp[Q];
                 qp36_moments(p.k1, p.k2, gr, qp);
-                collide36<Lane1>(f, r, F[0], F[1], F[2], p.ts, p.omts, qp, v2);
+                collide36<Lane1, REF>(f, r, F[0], F[1], F[2], p.ts, p.omts, qp, v2);
             } else {
-                collide36<Lane1>(f, r, F[0], F[1], F[2], p.ts, p.omts, nullptr, v2);
+                collide36<Lane1, REF>(f, r, F[0], F[1], F[2], p.ts, p.omts, nullptr, v2);
             }
             mv2 = fmaxf(mv2, v2);
 
@@ -843,7 +844,9 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
 // Many boxes in one persistent launch: each CTA takes (box, z tile, y tile,
 // x chunk) work items from an atomic counter until none are left.  Uneven
 // box sizes balance themselves; every box shares the tile shape and march.
-template <class S, int TY, int TZ, int L>
+// The boxes' parameters are read from global memory (REF: every box's rates
+// follow the reference's pattern, so the collision reads two of them).
+template <class S, int TY, int TZ, int L, bool REF>
 __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
     k_fused_collide_batch(const KParams<float> *__restrict__ params, const BatchBox *__restrict__ boxes,
                           int nbox, long long total_items, int P, int xl, unsigned int *counter)
@@ -875,8 +878,8 @@ __global__ void __launch_bounds__(TY *TZ, 768 / (TY * TZ))
         const int per_chunk = bx.tiles_z * bx.tiles_y;
         const int chunk = (int)(local / per_chunk), rem = (int)(local % per_chunk);
         const int ytile = rem / bx.tiles_z, ztile = rem % bx.tiles_z;
-        fused_tile<S, TY, TZ, L>(p, P, SlotShared<S>{slot_s}, bx.f0[P], bx.f0[1 - P], bx.rho[P], ztile * TZ,
-                                 ytile * TY, chunk * xl, xl, smem4);
+        fused_tile<S, TY, TZ, L, REF>(p, P, SlotShared<S>{slot_s}, bx.f0[P], bx.f0[1 - P], bx.rho[P],
+                                      ztile * TZ, ytile * TY, chunk * xl, xl, smem4);
         __syncthreads();
     }
 }

@@ -12,19 +12,6 @@ namespace pair_detail {
 template <int TY, int TZ, int L>
 constexpr size_t smem_bytes() { return PairRings<TY, TZ, L>::BYTES; }
 
-// The rates follow the reference's pattern: 1 except one value for moments
-// 2, 4, 6, 8 and one for 9, 11, 13, 14, 15 (FluidCuda.cu:154-157).
-inline bool reference_rates(const KParams<float> &p)
-{
-    for (int a : {0, 1, 3, 5, 7, 10, 12, 16, 17, 18})
-        if (p.ts[a] != 1.0f) return false;
-    for (int a : {4, 6, 8})
-        if (p.ts[a] != p.ts[2] || p.omts[a] != p.omts[2]) return false;
-    for (int a : {11, 13, 14, 15})
-        if (p.ts[a] != p.ts[9] || p.omts[a] != p.omts[9]) return false;
-    return true;
-}
-
 template <class S, int TY, int TZ, int L>
 void launch_t(const KParams<float> &p, int P, int xl, S *h, const float *f0c, float *f0n, const float *rho,
               cudaStream_t st)

@@ -16,7 +16,7 @@ void collide_t(const KParams<float> &p, S *h, const float *f0c, float *f0n, cons
     const dim3 grid((unsigned)((p.dz / 2 + NCZ - 1) / NCZ), (unsigned)((p.dy + NCY - 1) / NCY), (unsigned)p.dx);
     SlotTable<S> slots;
     for (int k = 0; k < Q - 1; ++k) slots.q[k] = h + (size_t)p.n * k;
-    if (pair_detail::reference_rates(p))
+    if (reference_rates(p))
         k_node_collide<S, P, true><<<grid, dim3(NCZ, NCY), 0, st>>>(p, slots, f0c, f0n, rho, F);
     else
         k_node_collide<S, P, false><<<grid, dim3(NCZ, NCY), 0, st>>>(p, slots, f0c, f0n, rho, F);

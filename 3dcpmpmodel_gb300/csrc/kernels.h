@@ -63,6 +63,19 @@ int fused_tile_count();
 FusedTile fused_tile(int idx, int xl);
 // The (storage, Laplacian, tile) instantiation fits this device's shared memory.
 bool fused_tile_usable(int storage, int lap_order, int ty, int tz, int np = 1, int form = 0);
+// The rates follow the reference's pattern: 1 except one value for moments
+// 2, 4, 6, 8 and one for 9, 11, 13, 14, 15 (FluidCuda.cu:154-157); the
+// collide kernels then take their compile-time case (collide36's REF).
+inline bool reference_rates(const KParams<float> &p)
+{
+    for (int a : {0, 1, 3, 5, 7, 10, 12, 16, 17, 18})
+        if (p.ts[a] != 1.0f) return false;
+    for (int a : {4, 6, 8})
+        if (p.ts[a] != p.ts[2] || p.omts[a] != p.omts[2]) return false;
+    for (int a : {11, 13, 14, 15})
+        if (p.ts[a] != p.ts[9] || p.omts[a] != p.omts[9]) return false;
+    return true;
+}
 // The paired kernel's grid requirement: DZ a multiple of 4.
 inline bool pair_grid_ok(int dz) { return dz % 4 == 0; }
 // Paired kernel (k_pair_<storage>.cu, one unit per storage type): each
@@ -88,6 +101,18 @@ CPMP_SPLIT_DECL(f16)
 CPMP_SPLIT_DECL(bf16)
 CPMP_SPLIT_DECL(f32)
 #undef CPMP_SPLIT_DECL
+// The batches' persistent one-node collide (k_batch_<storage>.cu): the
+// dynamic shared memory attribute of a tile, and one launch over every box
+// (ref: every box's rates follow the reference's pattern).
+#define CPMP_BATCH_DECL(SUFFIX)                                                                                  \
+    bool batch_set_attr_##SUFFIX(int lap_order, int ty, int tz, int max_smem);                                   \
+    void batch_collide_launch_##SUFFIX(int lap_order, const FusedTile &t, const KParams<float> *params,          \
+                                       const BatchBox *boxes, int nbox, long long total, int P,                  \
+                                       unsigned *counter, bool ref, cudaStream_t st);
+CPMP_BATCH_DECL(f16)
+CPMP_BATCH_DECL(bf16)
+CPMP_BATCH_DECL(f32)
+#undef CPMP_BATCH_DECL
 
 cudaError_t fused_setup_attributes();
 void fused_launch_init(int storage, const KParams<float> &p, const DropletDev &d, uint8_t *type,
@@ -109,10 +134,11 @@ void fused_launch_density(int storage, const KParams<float> &p, int P, const voi
 // pass.  params/boxes are device arrays of nbox entries; counter is one
 // device unsigned (reset here); wall_blocks / density_blocks are the sizes of
 // the flattened wall and density grids (each box's first block in
-// BatchBox::wblk0 / dblk0).
+// BatchBox::wblk0 / dblk0); ref_rates: every box's rates follow the
+// reference's pattern (reference_rates).
 void fused_batch_step(int storage, int lap_order, int wall_mode, int complex_bc, const FusedTile &t,
                       const KParams<float> *params, const BatchBox *boxes, int nbox, long long total_items,
-                      long long wall_blocks, long long density_blocks, int P, unsigned *counter,
+                      long long wall_blocks, long long density_blocks, int P, unsigned *counter, bool ref_rates,
                       cudaStream_t st, LaunchHook *hook);
 // Natural-order populations (post-stream at each node) to/from device
 // buffers of FP32 or FP64 (dst_is_f64).
