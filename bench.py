@@ -451,7 +451,7 @@ def run_batch(args, wl: dict, cp, torch) -> None:
     alg = bytes_per.get(dom_name, bytes_per["step"])
     achieved = alg * b.nodes / (dom_ms / dom_launches / 1e3) / 1e9
     peaks = measured_peaks()
-    bad = sum(1 for s in b.boxes if s.reduce(allow_nonfinite=True)["nonfinite"])
+    bad = sum(1 for d in b.reduce(allow_nonfinite=True) if d["nonfinite"])
 
     # ---- end to end through the public API with host buffers: every box's
     # populations uploaded from pinned host memory (FP32), K x (one batch step
