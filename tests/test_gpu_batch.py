@@ -99,3 +99,23 @@ def test_batch_reduce_equals_each_box_reduce(cpmp):
         assert got[0]["step"] == done
     assert got[0]["max_speed"] > 0 and got[5]["mass"] > 0
     b.close()
+
+
+def test_batch_reduce_reports_the_nonfinite_box(cpmp):
+    """A NaN density planted (from the host) on a fluid node of box 1 makes
+    cpmp_batch_reduce return CPMP_ERR_NONFINITE naming box 1, with every
+    box's diagnostics filled."""
+    b = cpmp.Batch([params_of(cpmp, box, "f32") for box in BOXES])
+    for s, box in zip(b.boxes, BOXES):
+        s.set_flow_field(radius=box["radius"], width=4.0)
+    b.step(2)
+    rho = b.boxes[1].get("rho")
+    rho[len(rho) // 2 + 5] = np.nan
+    b.boxes[1].set("rho", rho)
+    with pytest.raises(cpmp.CpmpError) as e:
+        b.reduce()
+    assert e.value.status == 5 and "box 1" in str(e.value)
+    got = b.reduce(allow_nonfinite=True)
+    assert [g["nonfinite"] for g in got] == [0, 1, 0]
+    assert got[0] == b.boxes[0].reduce() and got[2]["mass"] > 0
+    b.close()
