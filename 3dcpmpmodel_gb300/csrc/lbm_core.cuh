@@ -253,6 +253,20 @@ __device__ __forceinline__ void collide_mrt_edm(R f[Q], R rho, R ux, R uy, R uz,
         m[a] = v;
     }
     inverse_moments<R>(m, f);
+    if (sizeof(R) == 4) {
+        // FP32: the rest population is the remainder of the mass moment after
+        // the 18 moving populations (pairwise sums), so a node emits the mass
+        // it holds to one rounding.  The rounded reciprocal of 19 in
+        // inverse_moments gives every population m0 * fl(1/19), which raises
+        // each node's mass by 19 fl(1/19) - 1 = 7.5e-9 every step in FP32: a
+        // linear drift of the density (7.5e-6 after 1000 steps).  In exact
+        // arithmetic both forms give the same f0 (row 0 of M sums the
+        // populations); FP64 keeps the reference's expression.
+        const R a = (f[1] + f[2]) + (f[3] + f[4]) + (f[5] + f[6]);
+        const R b = ((f[7] + f[8]) + (f[9] + f[10])) + ((f[11] + f[12]) + (f[13] + f[14]));
+        const R c = (f[15] + f[16]) + (f[17] + f[18]);
+        f[0] = m[0] - ((a + c) + b);
+    }
 }
 
 }  // namespace cpmp

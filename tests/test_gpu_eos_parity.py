@@ -99,19 +99,21 @@ def test_laplace_probe_matches_oracle(cpmp, oracle_mod, cfg):
 
 
 # Measured maximum relative errors of FP32 runs against the FP64 reference
-# (walled CP-PRW box below):
+# (walled CP-PRW box below; velocities relative to the largest speed):
+#   steps          100      500      1000     2000
+#   PLAIN rho    1.7e-6   4.4e-6   5.2e-6   5.3e-6
+#   PLAIN u      2.2e-6   2.6e-6   3.8e-6   4.7e-6
 #   steps          10       100      200      500      1000
-#   PLAIN rho    5.9e-7   1.7e-6   3.6e-6   8.3e-6   1.8e-5
 #   FUSED rho    1.2e-6   9.5e-6   1.9e-5   2.5e-5   2.9e-5
 #   FUSED u      2.2e-6   8.5e-6   5.4e-6   7.0e-6   8.8e-6
-# The plain scheme (the reference's operator sequence in FP32) drifts about
-# linearly; the fused scheme balances mass without a rounded weight (each
-# node's rest population is the remainder of its new density, the density
-# pass divides by 36 with correct rounding), so its error levels off.  The
-# 1e-5 bound holds to about 500 steps (plain) and 100 steps (fused); after
-# 1000 steps the bounds asserted are those of the measured curve with a
-# margin of about 1.5.
-FP32_1000 = {"plain": (3e-5, 2e-5), "fused": (4.5e-5, 2e-5)}
+# Both schemes balance mass without a rounded weight: each node's rest
+# population is the remainder of its mass moment after the moving populations
+# (the PLAIN FP32 collide; the FUSED collide and its density pass in the
+# 36-scaled form), so neither error grows linearly.  The PLAIN form meets the
+# 1e-5 bound after 1000 steps (asserted here at 1e-5); the FUSED form levels
+# off near 3e-5 (an offset of the gas phase) and is asserted at its measured
+# curve with a margin of about 1.5.
+FP32_1000 = {"plain": (1e-5, 1e-5), "fused": (4.5e-5, 2e-5)}
 
 
 @pytest.mark.parametrize("scheme", ["plain", "fused"])
