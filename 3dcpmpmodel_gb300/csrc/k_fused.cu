@@ -312,7 +312,7 @@ void fused_launch_collide(int storage, const KParams<float> &p, int P, const Fus
 {
     if (t.form == 1) {
         hook_begin(hook, K_FORCE, st);
-        split_force_launch(p, t, rho, F, st);
+        split_force_launch(p, t, rho, F, storage == CPMP_STORE_F32, st);
         hook_end(hook, K_FORCE, st);
         hook_begin(hook, K_FUSED, st);
         if (storage == CPMP_STORE_F16)

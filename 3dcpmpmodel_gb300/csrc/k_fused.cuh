@@ -757,7 +757,7 @@ __device__ __forceinline__ void fused_tile(const KParams<float> &p, int P, const
             }
             const float r = pl[3][mc].x;
             float F[3], gr[3];
-            force_from_lines(lines, r, F, gr);
+            force_from_lines<sizeof(S) == 4>(lines, r, F, gr);  // exact scaling for FP32 storage
 
             // decode with the sources' rest populations as anchors: g = h + 3 a
             const float *fa[3] = {R.f0_plane(x - 1), R.f0_plane(x), R.f0_plane(x + 1)};

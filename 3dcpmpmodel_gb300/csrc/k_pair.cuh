@@ -417,8 +417,8 @@ __device__ __forceinline__ void pair_tile(const KParams<float> &p, int P, const 
             }
             const float4 cen = *reinterpret_cast<const float4 *>(rm_plane(x) + mc);
             float FA[3], FB[3], grA[3], grB[3];
-            force_from_lines(la, cen.x, FA, grA);
-            force_from_lines(lb, cen.z, FB, grB);
+            force_from_lines<sizeof(S) == 4>(la, cen.x, FA, grA);  // exact scaling for FP32 storage
+            force_from_lines<sizeof(S) == 4>(lb, cen.z, FB, grB);
             const float2 r = make_float2(cen.x, cen.z);
 
             // ---- decode with the sources' rest populations: g = h + 3 a

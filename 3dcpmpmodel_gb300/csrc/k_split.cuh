@@ -50,7 +50,8 @@ struct ForceRings {
 
 // F field layout: component c of node I at F[c * n + I]; components 0-2 the
 // force, 3-5 grad(rho) (written only with the K1/K2 term).
-template <int TY, int TZ, int L>
+// EXACT: the force scaling for FP32 storage (force_from_lines).
+template <int TY, int TZ, int L, bool EXACT>
 __device__ __forceinline__ void force_tile(const KParams<float> &p, const float *__restrict__ rho,
                                            float *__restrict__ F, const int z0, const int y0, const int x0,
                                            const int xl, float4 *smem4)
@@ -209,8 +210,8 @@ __device__ __forceinline__ void force_tile(const KParams<float> &p, const float 
             }
             const float4 cen = *reinterpret_cast<const float4 *>(rm_plane(x) + mc);
             float FA[3], FB[3], grA[3], grB[3];
-            force_from_lines(la, cen.x, FA, grA);
-            force_from_lines(lb, cen.z, FB, grB);
+            force_from_lines<EXACT>(la, cen.x, FA, grA);
+            force_from_lines<EXACT>(lb, cen.z, FB, grB);
             const int gx = wrap_small(x, p.dx);
             float *out = F + ((size_t)gx * plane + (size_t)(gy * p.dz + gz));
 #pragma unroll
@@ -235,12 +236,12 @@ __device__ __forceinline__ void force_tile(const KParams<float> &p, const float 
 
 // Registers: at most 128 per thread with 256 threads; shared memory decides
 // how many CTAs share an SM.
-template <int TY, int TZ, int L>
+template <int TY, int TZ, int L, bool EXACT>
 __global__ void __launch_bounds__(TY *TZ / 2, pair_min_blocks<TY * TZ / 2>())
     k_force_pass(KParams<float> p, const float *__restrict__ rho, float *__restrict__ F, int xl)
 {
     extern __shared__ __align__(128) float4 smem4[];
-    force_tile<TY, TZ, L>(p, rho, F, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl, smem4);
+    force_tile<TY, TZ, L, EXACT>(p, rho, F, blockIdx.x * TZ, blockIdx.y * TY, blockIdx.z * xl, xl, smem4);
 }
 
 // --------------------------------------------------------- collide pass ----

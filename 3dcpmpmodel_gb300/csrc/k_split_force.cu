@@ -16,8 +16,10 @@ struct ForceAttr {
     {
         const size_t b = force_smem<TY, TZ, L>();
         if ((int)b > max_smem) return false;
-        const bool ok = cudaFuncSetAttribute(k_force_pass<TY, TZ, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)b) == cudaSuccess;
+        const bool ok = cudaFuncSetAttribute(k_force_pass<TY, TZ, L, false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b) == cudaSuccess &&
+                        cudaFuncSetAttribute(k_force_pass<TY, TZ, L, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b) == cudaSuccess;
         cudaGetLastError();
         return ok;
     }
@@ -27,12 +29,16 @@ struct ForceLaunch {
     int xl;
     const float *rho;
     float *F;
+    bool exact;
     cudaStream_t st;
     template <class S, int TY, int TZ, int L>
     bool operator()()
     {
         const dim3 grid((p->dz + TZ - 1) / TZ, (p->dy + TY - 1) / TY, (p->dx + xl - 1) / xl);
-        k_force_pass<TY, TZ, L><<<grid, TY * TZ / 2, force_smem<TY, TZ, L>(), st>>>(*p, rho, F, xl);
+        if (exact)
+            k_force_pass<TY, TZ, L, true><<<grid, TY * TZ / 2, force_smem<TY, TZ, L>(), st>>>(*p, rho, F, xl);
+        else
+            k_force_pass<TY, TZ, L, false><<<grid, TY * TZ / 2, force_smem<TY, TZ, L>(), st>>>(*p, rho, F, xl);
         return true;
     }
 };
@@ -45,9 +51,10 @@ bool split_force_set_attr(int lap_order, int ty, int tz, int max_smem)
     return lap_order == 7 ? pair_detail::by_shape<float, 3>(ty, tz, f) : pair_detail::by_shape<float, 2>(ty, tz, f);
 }
 
-bool split_force_launch(const KParams<float> &p, const FusedTile &t, const float *rho, float *F, cudaStream_t st)
+bool split_force_launch(const KParams<float> &p, const FusedTile &t, const float *rho, float *F, bool exact,
+                        cudaStream_t st)
 {
-    ForceLaunch f{&p, t.xl, rho, F, st};
+    ForceLaunch f{&p, t.xl, rho, F, exact, st};
     return p.lap_order == 7 ? pair_detail::by_shape<float, 3>(t.ty, t.tz, f)
                             : pair_detail::by_shape<float, 2>(t.ty, t.tz, f);
 }

@@ -93,7 +93,9 @@ CPMP_PAIR_DECL(f32)
 // paired column tile (ty, tz) and march xl; false when (ty, tz) is not one of
 // its shapes.
 bool split_force_set_attr(int lap_order, int ty, int tz, int max_smem);
-bool split_force_launch(const KParams<float> &p, const FusedTile &t, const float *rho, float *F, cudaStream_t st);
+// exact: the force scaling for FP32 storage (force_from_lines).
+bool split_force_launch(const KParams<float> &p, const FusedTile &t, const float *rho, float *F, bool exact,
+                        cudaStream_t st);
 #define CPMP_SPLIT_DECL(SUFFIX)                                                                                  \
     void split_collide_launch_##SUFFIX(const KParams<float> &p, int P, void *h, const float *f0c, float *f0n,   \
                                        const float *rho, const float *F, cudaStream_t st);

@@ -157,6 +157,25 @@ __device__ __forceinline__ float2 line_term(float2 acc, float c, float2 a, float
 {
     return __ffma2_rn(make_float2(c, c), __fadd2_rn(a, make_float2(-b.x, -b.y)), acc);
 }
+// x / d for the force's constant divisors, as x Ch + RN(x Cl) with Ch =
+// RN(1/d) and Cl = RN(1/d - Ch): one multiply and one fused multiply-add (the
+// double-word constant multiplication of Brisebarre and Muller, "Correctly
+// rounded multiplication by arbitrary precision constants", IEEE Trans.
+// Computers 57(2), 2008).  For d = 360 and d = 3 it gives the correctly
+// rounded quotient (tests/test_scaling_constants.py checks the method and the
+// constants with exact rational arithmetic).
+__device__ __forceinline__ float div360(float x) { return fmaf(x, 0x1.6c16c2p-9f, x * -0x1.27d27ep-34f); }
+__device__ __forceinline__ float div3(float x) { return fmaf(x, 0x1.555556p-2f, x * -0x1.555556p-27f); }
+
+// EXACT (FP32 storage): the stencil sums are divided by 360 and grad(rho) by
+// 3 with correct rounding (div360, div3).  Multiplying by the rounded
+// reciprocals instead scales both gradients by 360 fl(1/360) = 1 + 2.4e-8 and
+// the ideal term by 3 fl(1/3) = 1 + 3.0e-8 in FP32: a bias of one sign on every
+// node, which moves the steady state (with it the FP32 density settled 2.9e-5
+// from the FP64 reference on a walled droplet box, without it within 2.3e-6).
+// FP16 / BF16 storage round the populations to 4.9e-4 / 3.9e-3 every step and
+// keep the single multiplications.
+template <bool EXACT = false>
 __device__ __forceinline__ void force_from_lines(const float2 l[9], float r, float F[3], float gr[3])
 {
     const float2 two = make_float2(2.f, 2.f), z = make_float2(0.f, 0.f);
@@ -174,6 +193,15 @@ __device__ __forceinline__ void force_from_lines(const float2 l[9], float r, flo
     g2 = __fadd2_rn(g2, l[7]);
     g1 = __fadd2_rn(g1, l[8]);
     g2 = __fadd2_rn(g2, neg(l[8]));
+    if (EXACT) {
+        gr[0] = div360(g0.x);
+        gr[1] = div360(g1.x);
+        gr[2] = div360(g2.x);
+        F[0] = fmaf(-div360(g0.y), r, div3(gr[0]));
+        F[1] = fmaf(-div360(g1.y), r, div3(gr[1]));
+        F[2] = fmaf(-div360(g2.y), r, div3(gr[2]));
+        return;
+    }
     const float inv360 = 1.0f / 360.0f;
     gr[0] = g0.x * inv360;
     gr[1] = g1.x * inv360;

@@ -4,9 +4,9 @@ kernels (golden fixtures) and the FP64 oracle.
 Tolerances (relative unless stated):
   PLAIN FP64 vs reference fixture / oracle      1e-11 (different summation
       order in the factored MRT; CUDA's log/tanh within an ulp of glibc's)
-  PLAIN FP32 vs FP64 oracle, rho                2e-5 after 200 steps
-  FUSED FP32 / FP16 / BF16 vs FP64 oracle, rho  2e-5 / 2e-3 / 1.5e-2 after 100 steps
-  velocities: max |du| / max |u_oracle|         scaled 20x the rho bound
+  PLAIN FP32 vs FP64 oracle, rho / u            1e-5 / 1e-4 after 200 steps
+  FUSED FP32 / FP16 / BF16 vs FP64 oracle, rho  5e-6 / 2e-3 / 1.5e-2 after 100 steps
+  velocities: max |du| / max |u_oracle|         scaled 20x the rho bound (FUSED)
 """
 import json
 import os
@@ -109,12 +109,12 @@ def test_plain_fp32_vs_fp64_oracle(cpmp, oracle_mod, cfg, steps):
     s = solver_for(cpmp, cfg, storage="f32", den=den)
     s.step(steps)
     fluid = st.type == 1
-    assert rel_err(s.get("rho"), st.dens, fluid) < 2e-5
-    assert vel_err(s.get("u"), (st.vx, st.vy, st.vz), fluid) < 4e-4
+    assert rel_err(s.get("rho"), st.dens, fluid) < 1e-5
+    assert vel_err(s.get("u"), (st.vx, st.vy, st.vz), fluid) < 1e-4
     s.close()
 
 
-@pytest.mark.parametrize("storage,rtol", [("f32", 2e-5), ("f16", 2e-3), ("bf16", 1.5e-2)])
+@pytest.mark.parametrize("storage,rtol", [("f32", 5e-6), ("f16", 2e-3), ("bf16", 1.5e-2)])
 @pytest.mark.parametrize("cfg", [WALLED, PERIODIC_CS], ids=["walled_prw", "periodic_cs"])
 def test_fused_vs_fp64_oracle(cpmp, oracle_mod, storage, rtol, cfg):
     steps = 100
@@ -154,8 +154,9 @@ def test_mass_conservation(cpmp, scheme, storage):
     m0 = s.reduce()["mass"]
     s.step(300)
     m1 = s.reduce()["mass"]
-    # FP32 rounding is systematic in a near-steady state (the same error every
-    # step), so the drift grows linearly; FP64 shows the exact conservation.
+    # FP32 and below: each rest population is the remainder of its node's mass
+    # moment, so the mass changes only by roundings of varying sign; FP64
+    # shows the exact conservation.
     tol = {"f64": 1e-12, "f32": 1e-5, "f16": 2e-4, "bf16": 2e-3}[storage]
     assert abs(m1 - m0) <= tol * m0, (m0, m1)
     s.close()
