@@ -138,7 +138,7 @@ __device__ __forceinline__ void density_node(const KParams<float> &p, int P, con
     }
     float ES, DS;
     mass_sums<Lane1>(g, ES, DS);
-    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
+    rho[I] = a0 + div36(fmaf(2.f, ES, DS));
 }
 
 // Two stored values of consecutive nodes as a float pair: one vector load
@@ -289,7 +289,7 @@ __device__ __forceinline__ void density_pair_fast(const KParams<float> &p, const
     float2 ES, DS;
     mass_sums<Lane2>(g, ES, DS);
     const float2 a0 = *reinterpret_cast<const float2 *>(f0 + I);
-    const float2 r = Lane2::add(a0, Lane2::div_rn(Lane2::fma(Lane2::k(2.f), ES, DS), 36.f));
+    const float2 r = Lane2::add(a0, Lane2::div36(Lane2::fma(Lane2::k(2.f), ES, DS)));
     if (botw) rho[I + 1] = r.y;       // node I is on the bottom wall layer
     else if (topw) rho[I] = r.x;      // node I + 1 is on the top wall layer
     else *reinterpret_cast<float2 *>(rho + I) = r;
@@ -319,7 +319,7 @@ __device__ __forceinline__ void density_wall_node(const KParams<float> &p, int P
     for (int q = 1; q < Q; ++q) g[q] = fmaf(3.f, a[q - 1], hv[q - 1]);
     float ES, DS;
     mass_sums<Lane1>(g, ES, DS);
-    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
+    rho[I] = a0 + div36(fmaf(2.f, ES, DS));
 }
 
 // density_wall_node for a fluid node of an x or y edge column of a walled
@@ -345,7 +345,7 @@ __device__ __forceinline__ void density_edge_node(const KParams<float> &p, int P
     for (int q = 1; q < Q; ++q) g[q] = fmaf(3.f, a[q - 1], hv[q - 1]);
     float ES, DS;
     mass_sums<Lane1>(g, ES, DS);
-    rho[I] = a0 + __fdiv_rn(fmaf(2.f, ES, DS), 36.f);
+    rho[I] = a0 + div36(fmaf(2.f, ES, DS));
 }
 
 // Density of the nodes k0 and k0 + 1 of column (i, j) (either may lie

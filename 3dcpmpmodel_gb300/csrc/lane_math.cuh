@@ -25,6 +25,23 @@
 
 namespace cpmp {
 
+// x / d for the constant divisors of the FUSED arithmetic, as x Ch + RN(x Cl)
+// with Ch = RN(1/d) and Cl = RN(1/d - Ch): one multiply and one fused
+// multiply-add (the double-word constant multiplication of Brisebarre and
+// Muller, "Correctly rounded multiplication by arbitrary precision constants",
+// IEEE Trans. Computers 57(2), 2008).  For d = 3, 36 and 360 it gives the
+// correctly rounded quotient of every FP32 x with |x| >= 2^-93 (where x Cl
+// stays normal): tests/test_scaling_constants.py checks the constants and the
+// method with exact integer arithmetic over every eighth mantissa of a binade
+// (the rounding does not depend on the binade), and a sweep of every mantissa
+// found no difference either.
+__device__ __forceinline__ float div3(float x) { return __fmaf_rn(x, 0x1.555556p-2f, __fmul_rn(x, -0x1.555556p-27f)); }
+__device__ __forceinline__ float div36(float x) { return __fmaf_rn(x, 0x1.c71c72p-6f, __fmul_rn(x, -0x1.c71c72p-33f)); }
+__device__ __forceinline__ float div360(float x)
+{
+    return __fmaf_rn(x, 0x1.6c16c2p-9f, __fmul_rn(x, -0x1.27d27ep-34f));
+}
+
 struct Lane1 {
     using V = float;
     static __device__ __forceinline__ V k(float c) { return c; }
@@ -39,7 +56,7 @@ struct Lane1 {
     static __device__ __forceinline__ V rcp(V a) { return __fdividef(1.0f, a); }
     static __device__ __forceinline__ V lg2(V a) { return __log2f(a); }
     static __device__ __forceinline__ V rcp_rn(V a) { return __frcp_rn(a); }
-    static __device__ __forceinline__ V div_rn(V a, float d) { return __fdiv_rn(a, d); }
+    static __device__ __forceinline__ V div36(V a) { return cpmp::div36(a); }
 };
 
 struct Lane2 {
@@ -58,7 +75,11 @@ struct Lane2 {
     static __device__ __forceinline__ V rcp(V a) { return make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
     static __device__ __forceinline__ V lg2(V a) { return make_float2(__log2f(a.x), __log2f(a.y)); }
     static __device__ __forceinline__ V rcp_rn(V a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
-    static __device__ __forceinline__ V div_rn(V a, float d) { return make_float2(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d)); }
+    static __device__ __forceinline__ V div36(V a)
+    {
+        return __ffma2_rn(a, make_float2(0x1.c71c72p-6f, 0x1.c71c72p-6f),
+                          __fmul2_rn(a, make_float2(-0x1.c71c72p-33f, -0x1.c71c72p-33f)));
+    }
 };
 
 // ---------------------------------------------------------------- EOS ----
@@ -157,16 +178,6 @@ __device__ __forceinline__ float2 line_term(float2 acc, float c, float2 a, float
 {
     return __ffma2_rn(make_float2(c, c), __fadd2_rn(a, make_float2(-b.x, -b.y)), acc);
 }
-// x / d for the force's constant divisors, as x Ch + RN(x Cl) with Ch =
-// RN(1/d) and Cl = RN(1/d - Ch): one multiply and one fused multiply-add (the
-// double-word constant multiplication of Brisebarre and Muller, "Correctly
-// rounded multiplication by arbitrary precision constants", IEEE Trans.
-// Computers 57(2), 2008).  For d = 360 and d = 3 it gives the correctly
-// rounded quotient (tests/test_scaling_constants.py checks the method and the
-// constants with exact rational arithmetic).
-__device__ __forceinline__ float div360(float x) { return fmaf(x, 0x1.6c16c2p-9f, x * -0x1.27d27ep-34f); }
-__device__ __forceinline__ float div3(float x) { return fmaf(x, 0x1.555556p-2f, x * -0x1.555556p-27f); }
-
 // EXACT (FP32 storage): the stencil sums are divided by 360 and grad(rho) by
 // 3 with correct rounding (div360, div3).  Multiplying by the rounded
 // reciprocals instead scales both gradients by 360 fl(1/360) = 1 + 2.4e-8 and
@@ -431,7 +442,7 @@ __device__ __forceinline__ void collide36(typename O::V g[Q], typename O::V rho,
     // node emits exactly (up to the last rounding) the mass it keeps
     V ES, DS;
     mass_sums<O>(g, ES, DS);
-    g[0] = O::div_rn(O::sub(m[0], O::fma(O::k(2.f), ES, DS)), 36.f);
+    g[0] = O::div36(O::sub(m[0], O::fma(O::k(2.f), ES, DS)));
 }
 
 // 36 x the K1/K2 pressure-tensor moments Qp (FluidCuda.cu:260-266) from
